@@ -1,0 +1,174 @@
+/*
+ * sg_solver.h -- C ABI of the GB300 solve path for SPECFEM3D_GEOTECH.
+ *
+ * Every entry point is plain C: integers, doubles and pointers to host
+ * arrays, no CUDA or torch types.  Each call returns an errcode (SG_OK = 0)
+ * and, where the reference has one, fills a blank-padded Fortran-style
+ * errtag of SG_ERRTAG_LEN characters.  Array layouts follow the reference:
+ *   - global vectors are 0:neq (length neq+1); index 0 is the sink of the
+ *     constrained dofs and holds 0;
+ *   - element matrices k(nedof,nedof,nelmt) are column-major, element e's
+ *     81x81 block is 6561 consecutive doubles, k[(e*81 + col)*81 + row];
+ *   - gdof_elmt(nedof,nelmt): gdof_elmt[e*81 + a] in [0,neq], 0 = fixed,
+ *     dofs node-major inside an element [n1x n1y n1z n2x ...];
+ *   - hex8 connectivity is 1-based in Exodus/CUBIT corner order, material ids
+ *     are 1-based, face ids 1..6 follow src/element.f90:48-141.
+ * A context (sg_ctx) owns the device, a stream and all device memory; one
+ * context is used by one host thread at a time.
+ */
+#ifndef SG_SOLVER_H
+#define SG_SOLVER_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SG_ERRTAG_LEN 250
+
+enum sg_status {
+  SG_OK = 0,
+  SG_ERR_NOCONV = -1,   /* PCG did not converge: same code as the reference's errcode -1 */
+  SG_ERR_TIMEOUT = -2,  /* a device loop hit its wall-clock or iteration guard */
+  SG_ERR_OOM = -3,      /* the request does not fit the context's HBM budget */
+  SG_ERR_BADARG = -4,   /* invalid sizes, indices or options */
+  SG_ERR_CUDA = -5,     /* a CUDA runtime error; see sg_last_error */
+  SG_ERR_NODEVICE = -6  /* no CUDA device / the kernels are not loadable */
+};
+
+/* Precision forms of the device-resident solve. */
+enum sg_precision {
+  SG_PREC_FP64 = 0,   /* plain: FP64 element matrices, FP64 PCG (the drop-in semantics) */
+  SG_PREC_MIXED = 1   /* FP32 element matrices and FP32 PCG, FP64 iterative refinement */
+};
+
+typedef struct sg_ctx sg_ctx;
+typedef struct sg_model sg_model;
+
+/* ---- context ---------------------------------------------------------- */
+/* Creates a context on CUDA device `device`.  hbm_budget = 0 means all free
+ * device memory.  Returns NULL if no device is usable (sg_create_status tells why). */
+sg_ctx* sg_create(int device, size_t hbm_budget);
+int sg_create_status(void);
+void sg_destroy(sg_ctx* ctx);
+const char* sg_last_error(const sg_ctx* ctx);
+/* Device memory currently held by the context, bytes. */
+size_t sg_hbm_used(const sg_ctx* ctx);
+
+/* ---- the plain drop-in: pcg_solver ------------------------------------ */
+/* Replaces subroutine pcg_solver(neq,nelmt,k,u,f,dprecon,gdof_elmt,cg_iter,
+ * errcode,errtag) of module solver (src/solver.f90:14-79); the module globals
+ * cg_maxiter, cg_tol and nedof (src/solver.f90:8) are passed explicitly.
+ * Diagonally preconditioned CG on the element-by-element operator, warm start
+ * from u when max|u| > 0, stop when |alpha|*max|p|/max|u| <= cg_tol.  Only u
+ * is modified.  Returns SG_OK (cg_iter = stopping iteration) or
+ * SG_ERR_NOCONV with errtag "ERROR: PCG solver doesn't converge!". */
+int sg_pcg_solve(sg_ctx* ctx, int neq, int nelmt, int nedof, const double* k, double* u,
+                 const double* f, const double* dprecon, const int* gdof_elmt, int cg_maxiter,
+                 double cg_tol, int* cg_iter, char* errtag);
+
+/* ---- device-resident model -------------------------------------------- */
+/* Builds a spectral (27-node) model from an 8-node hex mesh: hex2spec with
+ * node merging (src/mesh_spec.f90:17-386), face constraints and node-major dof
+ * numbering (src/apply_bc.f90:7-143), then uploads the mesh and builds the
+ * element matrices, diagonal preconditioner and gravity load on the device
+ * (src/preprocess.f90:74-148).
+ *   props: nmatblk rows of [gamma E nu phi c psi] (src/read_input.f90:563-595)
+ *   bc_counts[3]: number of (element,face) pairs fixing ux, uy, uz
+ *   bc_pairs: the pairs, ux list then uy then uz, 2 ints each
+ *   precision: SG_PREC_FP64 or SG_PREC_MIXED (which element-matrix copies to keep) */
+sg_model* sg_model_from_hex8(sg_ctx* ctx, int nnode8, const double* x8, const double* y8,
+                             const double* z8, int nelmt, const int* conn8, const int* mat_id,
+                             int nmatblk, const double* props, const int* bc_counts,
+                             const int* bc_pairs, int precision, char* errtag);
+/* Reads a serial .sem deck (preinfo/mesh/bc/material/control/stress0 lines,
+ * src/read_input.f90:13-619) and builds the model as above. */
+sg_model* sg_model_from_deck(sg_ctx* ctx, const char* sem_path, int precision, char* errtag);
+void sg_model_free(sg_model* model);
+/* info[0..7] = nnode, nelmt, neq, nmatblk, nsrf (deck), ngroups, 0, 0 */
+int sg_model_info(const sg_model* model, int* info);
+/* Host copies of the spectral mesh (any pointer may be NULL):
+ * g_coord[3*nnode], g_num[27*nelmt] (0-based nodes), gdof[3*nnode], gdof_elmt[81*nelmt]. */
+int sg_model_arrays(const sg_model* model, double* g_coord, int* g_num, int* gdof, int* gdof_elmt);
+/* Deck control values: dctl = {cg_tol, nl_tol}, ictl = {cg_maxiter, nl_maxiter, phinu,
+ * allelastic, nexcav, ninc}, srf (nsrf doubles, may be NULL). */
+int sg_model_control(const sg_model* model, double* dctl, int* ictl, double* srf);
+/* Element matrices (column-major 81x81 per element, FP64), diagonal
+ * dprecon (0:neq, before inversion) and gravity load extload (0:neq) as built on
+ * the device by stiffness_bodyload; any pointer may be NULL. */
+int sg_model_stiffness(sg_model* model, double* storekm, double* dprecon, double* extload);
+
+/* ---- one strength-reduction trial of slope3d (src/slope.F90:244-443) ---- */
+typedef struct sg_control {
+  double cg_tol;       /* PCG step tolerance (reference cg_tol) */
+  double nl_tol;       /* plastic-iteration tolerance (reference nl_tol) */
+  int cg_maxiter;
+  int nl_maxiter;
+  int phinu;           /* phi-nu correction of strength_reduction */
+  int allelastic;
+  int precision;       /* sg_precision */
+  int reserved;
+  double refine_rtol;  /* SG_PREC_MIXED: FP64 relative residual target (default 1e-10) */
+  double inner_rtol;   /* SG_PREC_MIXED: FP32 inner PCG residual reduction per refinement (default 1e-4) */
+} sg_control;
+
+typedef struct sg_trial_result {
+  double srf;
+  int cg_tot;          /* summed PCG iterations (summary column CGITER) */
+  int nl_iter;         /* plastic iterations (summary column NLITER) */
+  int converged;       /* nl_isconv at exit */
+  int failed;          /* nl_iter == nl_maxiter: the SRF loop's exit test */
+  double uxmax, umax, fmax, uerr;
+  int errcode;         /* SG_OK or the PCG error */
+  int refine_steps;    /* SG_PREC_MIXED: FP64 residual evaluations */
+  double seconds;      /* device wall time of the trial */
+} sg_trial_result;
+
+/* Runs k independent SRF trials of the model's mesh concurrently (k = 1 is
+ * the plain one-at-a-time slope3d trial).  Trials share the element matrices
+ * and are batched as k right-hand sides of the element apply; each keeps its
+ * own factored properties, plastic strain, stress, body load and iteration
+ * counts.  Valid only when the stiffness does not depend on the SRF
+ * (phinu = 0 or no phi-nu correction triggered); otherwise returns SG_ERR_BADARG.
+ * x_out (optional, k*(neq+1)) receives each trial's displacement. */
+int sg_srf_trials(sg_model* model, const sg_control* ctl, int k, const double* srf,
+                  sg_trial_result* results, double* x_out);
+
+/* Stress state of the last trial batch: stress[(t*nelmt + e)*27*6 + i*6 + s] for trial t. */
+int sg_last_stress(sg_model* model, int trial, double* stress_elmt);
+
+/* The slope3d SRF sweep: trials srf[0..nsrf) in order, stopping after the first
+ * failed trial (src/slope.F90:441).  Returns the number of trials run in *ndone. */
+int sg_srf_sweep(sg_model* model, const sg_control* ctl, int nsrf, const double* srf,
+                 sg_trial_result* results, int* ndone);
+
+/* Critical SRF on the grid lo + step*m (m = 0..round((hi-lo)/step)), the
+ * smallest grid SRF whose trial fails, assuming lo is stable and hi fails.
+ * k = 1 is plain bisection; k > 1 probes k grid points per round (k-section)
+ * as one batched trial set.  *ntrials and *nrounds report the work done. */
+int sg_fos(sg_model* model, const sg_control* ctl, double lo, double hi, double step, int k,
+           double* fos, int* ntrials, int* nrounds);
+
+/* ---- staged excavation (src/excavation.F90:15-709), nsrf = 1 ---------- */
+/* s0_type 1: overburden initial stress s0 - gamma*|z - z0| with K0
+ * (src/postprocess.f90:10-33); s0_type 0: elastic gravity solve
+ * (src/excavation.F90:182-238).  nexcavid[i] ids per stage, excavid the ids.
+ * stage_res: nexcav rows of [stage cg_tot nl_tot uxmax umax fmax failed errcode].
+ * Returns the number of stages run in *nstage. */
+int sg_excavation(sg_model* model, const sg_control* ctl, int s0_type, double z0, double s0,
+                  double k0, int nexcav, const int* nexcavid, const int* excavid, int ninc,
+                  double srf, double* stage_res, int* nstage);
+
+/* ---- timing of the device work of the last call ----------------------- */
+/* ms[0] total, ms[1] element apply, ms[2] gather, ms[3] PCG vector update,
+ * ms[4] stress update, ms[5] stiffness build; counts[0..3] = launches of the
+ * apply kernel, total kernel launches, PCG iterations, FP64 refinement residuals.
+ * Collected with CUDA events on the context's stream when enabled. */
+int sg_profile_enable(sg_ctx* ctx, int on);
+int sg_profile_read(sg_ctx* ctx, double* ms, long long* counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SG_SOLVER_H */

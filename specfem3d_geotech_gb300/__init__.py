@@ -1,0 +1,316 @@
+"""GB300 solve path of SPECFEM3D_GEOTECH behind a C ABI.
+
+The product is the CUDA library ``_lib/libsg.so`` (sources in ``csrc/``,
+declarations in ``include/sg_solver.h``).  This package is a thin ctypes
+mirror of that ABI for Python callers and tests:
+
+* :func:`pcg_solver` -- the reference's ``pcg_solver`` contract
+  (src/solver.f90:14-79): same arguments, ``u`` updated in place, returns
+  ``(cg_iter, errcode, errtag)`` with errcode 0 / -1 like the Fortran.
+* :class:`Model` -- a device-resident spectral model built from a hex8 mesh
+  or a ``.sem`` deck, with slope3d trials, SRF sweeps, factor-of-safety
+  search and staged excavation.
+
+There is no CPU fallback: if the library cannot be loaded or no CUDA device
+is present the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import meshgen  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libsg.so")
+ERRTAG_LEN = 250
+
+SG_OK, SG_ERR_NOCONV, SG_ERR_TIMEOUT, SG_ERR_OOM, SG_ERR_BADARG, SG_ERR_CUDA, SG_ERR_NODEVICE = 0, -1, -2, -3, -4, -5, -6
+PREC_FP64, PREC_MIXED = 0, 1
+
+EXPORTED = (
+    "sg_create", "sg_create_status", "sg_destroy", "sg_last_error", "sg_hbm_used", "sg_pcg_solve",
+    "sg_model_from_hex8", "sg_model_from_deck", "sg_model_free", "sg_model_info", "sg_model_arrays",
+    "sg_model_control", "sg_model_stiffness", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
+    "sg_excavation", "sg_profile_enable", "sg_profile_read",
+)
+
+
+class SgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class Control(C.Structure):
+    """sg_control (include/sg_solver.h)."""
+
+    _fields_ = [("cg_tol", C.c_double), ("nl_tol", C.c_double), ("cg_maxiter", C.c_int), ("nl_maxiter", C.c_int),
+                ("phinu", C.c_int), ("allelastic", C.c_int), ("precision", C.c_int), ("reserved", C.c_int),
+                ("refine_rtol", C.c_double), ("inner_rtol", C.c_double)]
+
+
+class TrialResult(C.Structure):
+    """sg_trial_result (include/sg_solver.h)."""
+
+    _fields_ = [("srf", C.c_double), ("cg_tot", C.c_int), ("nl_iter", C.c_int), ("converged", C.c_int),
+                ("failed", C.c_int), ("uxmax", C.c_double), ("umax", C.c_double), ("fmax", C.c_double),
+                ("uerr", C.c_double), ("errcode", C.c_int), ("refine_steps", C.c_int), ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib(path: Optional[str] = None):
+    """Load libsg.so (built by ``build.build()``); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise OSError(f"{path} not built: run specfem3d_geotech_gb300.build.build()")
+    L = C.CDLL(path)
+    vp, i, d, sz = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+    L.sg_create.restype = vp
+    L.sg_create.argtypes = [i, sz]
+    L.sg_create_status.restype = i
+    L.sg_destroy.argtypes = [vp]
+    L.sg_last_error.restype = C.c_char_p
+    L.sg_last_error.argtypes = [vp]
+    L.sg_hbm_used.restype = sz
+    L.sg_hbm_used.argtypes = [vp]
+    L.sg_pcg_solve.restype = i
+    L.sg_pcg_solve.argtypes = [vp, i, i, i, vp, vp, vp, vp, vp, i, d, C.POINTER(C.c_int), C.c_char_p]
+    L.sg_model_from_hex8.restype = vp
+    L.sg_model_from_hex8.argtypes = [vp, i, vp, vp, vp, i, vp, vp, i, vp, vp, vp, i, C.c_char_p]
+    L.sg_model_from_deck.restype = vp
+    L.sg_model_from_deck.argtypes = [vp, C.c_char_p, i, C.c_char_p]
+    L.sg_model_free.argtypes = [vp]
+    L.sg_model_info.restype = i
+    L.sg_model_info.argtypes = [vp, vp]
+    L.sg_model_arrays.restype = i
+    L.sg_model_arrays.argtypes = [vp, vp, vp, vp, vp]
+    L.sg_model_control.restype = i
+    L.sg_model_control.argtypes = [vp, vp, vp, vp]
+    L.sg_model_stiffness.restype = i
+    L.sg_model_stiffness.argtypes = [vp, vp, vp, vp]
+    L.sg_srf_trials.restype = i
+    L.sg_srf_trials.argtypes = [vp, C.POINTER(Control), i, vp, vp, vp]
+    L.sg_last_stress.restype = i
+    L.sg_last_stress.argtypes = [vp, i, vp]
+    L.sg_srf_sweep.restype = i
+    L.sg_srf_sweep.argtypes = [vp, C.POINTER(Control), i, vp, vp, C.POINTER(C.c_int)]
+    L.sg_fos.restype = i
+    L.sg_fos.argtypes = [vp, C.POINTER(Control), d, d, d, i, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                         C.POINTER(C.c_int)]
+    L.sg_excavation.restype = i
+    L.sg_excavation.argtypes = [vp, C.POINTER(Control), i, d, d, d, i, vp, vp, i, d, vp, C.POINTER(C.c_int)]
+    L.sg_profile_enable.restype = i
+    L.sg_profile_enable.argtypes = [vp, i]
+    L.sg_profile_read.restype = i
+    L.sg_profile_read.argtypes = [vp, vp, vp]
+    _lib = L
+    return L
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data
+
+
+class Context:
+    """sg_ctx: one CUDA device, one stream, the device memory of its models."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        L = lib()
+        self.h = L.sg_create(device, hbm_budget)
+        if not self.h:
+            raise SgError(L.sg_create_status(), "sg_create: no usable CUDA device")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sg_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    @property
+    def last_error(self) -> str:
+        return lib().sg_last_error(self.h).decode()
+
+    @property
+    def hbm_used(self) -> int:
+        return int(lib().sg_hbm_used(self.h))
+
+    def profile(self, on: bool = True):
+        lib().sg_profile_enable(self.h, 1 if on else 0)
+
+    def profile_read(self):
+        ms = np.zeros(8)
+        cnt = np.zeros(4, np.int64)
+        lib().sg_profile_read(self.h, _ptr(ms), _ptr(cnt))
+        return dict(total_ms=ms[0], apply_ms=ms[1], gather_ms=ms[2], update_ms=ms[3], stress_ms=ms[4],
+                    stiffness_ms=ms[5], apply_launches=int(cnt[0]), launches=int(cnt[1]), pcg_iters=int(cnt[2]),
+                    refine_residuals=int(cnt[3]))
+
+
+_default_ctx: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def pcg_solver(neq: int, nelmt: int, k: np.ndarray, u: np.ndarray, f: np.ndarray, dprecon: np.ndarray,
+               gdof_elmt: np.ndarray, cg_maxiter: int, cg_tol: float, ctx: Optional[Context] = None):
+    """Drop-in for ``pcg_solver(neq,nelmt,k,u,f,dprecon,gdof_elmt,cg_iter,errcode,errtag)``.
+
+    ``k`` holds the reference's k(81,81,nelmt) (element e's column-major block
+    at ``k[e]`` when shaped (nelmt, 81, 81) as [e, col, row]); ``u`` (neq+1,
+    float64, C-contiguous) is updated in place; ``gdof_elmt`` is (nelmt, 81)
+    int32 with 0 for constrained dofs.  Returns ``(cg_iter, errcode, errtag)``.
+    """
+    ctx = ctx or default_context()
+    if u.dtype != np.float64 or not u.flags.c_contiguous or u.shape[0] != neq + 1:
+        raise ValueError("u must be a C-contiguous float64 array of length neq+1")
+    k = np.ascontiguousarray(k, np.float64)
+    f = np.ascontiguousarray(f, np.float64)
+    dprecon = np.ascontiguousarray(dprecon, np.float64)
+    ge = np.ascontiguousarray(gdof_elmt, np.int32)
+    it = C.c_int(0)
+    tag = C.create_string_buffer(ERRTAG_LEN + 1)
+    err = lib().sg_pcg_solve(ctx.h, neq, nelmt, 81, _ptr(k), _ptr(u), _ptr(f), _ptr(dprecon), _ptr(ge), cg_maxiter,
+                             cg_tol, C.byref(it), tag)
+    if err not in (SG_OK, SG_ERR_NOCONV):
+        raise SgError(err, tag.value.decode().strip() or ctx.last_error)
+    return it.value, err, tag.value.decode().rstrip()
+
+
+def make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=2000, phinu=0, allelastic=0,
+                 precision=PREC_FP64, refine_rtol=1e-10, inner_rtol=1e-4) -> Control:
+    return Control(cg_tol, nl_tol, cg_maxiter, nl_maxiter, phinu, allelastic, precision, 0, refine_rtol, inner_rtol)
+
+
+class Model:
+    """A spectral model resident on the device (sg_model)."""
+
+    def __init__(self, mesh=None, deck: Optional[str] = None, precision: int = PREC_FP64,
+                 ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        self.precision = precision
+        L = lib()
+        tag = C.create_string_buffer(ERRTAG_LEN + 1)
+        if deck is not None:
+            self.h = L.sg_model_from_deck(self.ctx.h, deck.encode(), precision, tag)
+            self.mesh = None
+        else:
+            self.mesh = mesh
+            self._keep = [np.ascontiguousarray(mesh.x, np.float64), np.ascontiguousarray(mesh.y, np.float64),
+                          np.ascontiguousarray(mesh.z, np.float64),
+                          np.ascontiguousarray(mesh.conn.reshape(-1), np.int32),
+                          np.ascontiguousarray(mesh.mat_id, np.int32),
+                          np.ascontiguousarray(mesh.props.reshape(-1), np.float64),
+                          np.array([b.shape[0] for b in mesh.bc], np.int32),
+                          np.ascontiguousarray(np.concatenate(mesh.bc).reshape(-1), np.int32)]
+            x, y, z, conn, mid, props, cnt, pairs = self._keep
+            self.h = L.sg_model_from_hex8(self.ctx.h, mesh.nnode8, _ptr(x), _ptr(y), _ptr(z), mesh.nelmt, _ptr(conn),
+                                          _ptr(mid), mesh.props.shape[0], _ptr(props), _ptr(cnt), _ptr(pairs),
+                                          precision, tag)
+        if not self.h:
+            raise SgError(SG_ERR_BADARG, tag.value.decode().strip() or self.ctx.last_error)
+        info = np.zeros(8, np.int32)
+        L.sg_model_info(self.h, _ptr(info))
+        self.nnode, self.nelmt, self.neq, self.nmatblk, self.nsrf, self.ngroups = (int(v) for v in info[:6])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sg_model_free(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def arrays(self):
+        g_coord = np.zeros(3 * self.nnode)
+        g_num = np.zeros(27 * self.nelmt, np.int32)
+        gdof = np.zeros(3 * self.nnode, np.int32)
+        ge = np.zeros(81 * self.nelmt, np.int32)
+        lib().sg_model_arrays(self.h, _ptr(g_coord), _ptr(g_num), _ptr(gdof), _ptr(ge))
+        return dict(g_coord=g_coord.reshape(-1, 3), g_num=g_num.reshape(-1, 27), gdof=gdof.reshape(-1, 3),
+                    gdof_elmt=ge.reshape(-1, 81))
+
+    def deck_control(self):
+        d = np.zeros(2)
+        i = np.zeros(6, np.int32)
+        srf = np.zeros(max(self.nsrf, 1))
+        lib().sg_model_control(self.h, _ptr(d), _ptr(i), _ptr(srf))
+        return dict(cg_tol=d[0], nl_tol=d[1], cg_maxiter=int(i[0]), nl_maxiter=int(i[1]), phinu=int(i[2]),
+                    allelastic=int(i[3]), nexcav=int(i[4]), ninc=int(i[5]), srf=srf[: self.nsrf])
+
+    def stiffness(self, want_k: bool = True):
+        """(storekm[e, col, row], dprecon before inversion, extload) as built on the device."""
+        km = np.zeros(81 * 81 * self.nelmt) if want_k else None
+        dp = np.zeros(self.neq + 1)
+        ext = np.zeros(self.neq + 1)
+        st = lib().sg_model_stiffness(self.h, _ptr(km) if want_k else None, _ptr(dp), _ptr(ext))
+        if st:
+            raise SgError(st, self.ctx.last_error)
+        return (km.reshape(self.nelmt, 81, 81) if want_k else None), dp, ext
+
+    def trials(self, srf: Sequence[float], ctl: Control, want_x: bool = False):
+        srf = np.ascontiguousarray(srf, np.float64)
+        k = len(srf)
+        res = (TrialResult * k)()
+        x = np.zeros(k * (self.neq + 1)) if want_x else None
+        st = lib().sg_srf_trials(self.h, C.byref(ctl), k, _ptr(srf), C.cast(res, C.c_void_p),
+                                 _ptr(x) if want_x else None)
+        if st not in (SG_OK, SG_ERR_NOCONV):
+            raise SgError(st, self.ctx.last_error)
+        out = [r.as_dict() for r in res]
+        if want_x:
+            return out, x.reshape(k, self.neq + 1)
+        return out
+
+    def last_stress(self, trial: int = 0):
+        s = np.zeros(self.nelmt * 27 * 6)
+        st = lib().sg_last_stress(self.h, trial, _ptr(s))
+        if st:
+            raise SgError(st, "sg_last_stress")
+        return s.reshape(self.nelmt, 27, 6)
+
+    def sweep(self, srf: Sequence[float], ctl: Control):
+        srf = np.ascontiguousarray(srf, np.float64)
+        res = (TrialResult * len(srf))()
+        n = C.c_int(0)
+        st = lib().sg_srf_sweep(self.h, C.byref(ctl), len(srf), _ptr(srf), C.cast(res, C.c_void_p), C.byref(n))
+        if st not in (SG_OK, SG_ERR_NOCONV):
+            raise SgError(st, self.ctx.last_error)
+        return [res[i].as_dict() for i in range(n.value)]
+
+    def fos(self, ctl: Control, lo: float = 1.0, hi: float = 3.0, step: float = 0.01, k: int = 1):
+        v = C.c_double(0)
+        nt = C.c_int(0)
+        nr = C.c_int(0)
+        st = lib().sg_fos(self.h, C.byref(ctl), lo, hi, step, k, C.byref(v), C.byref(nt), C.byref(nr))
+        if st:
+            raise SgError(st, self.ctx.last_error)
+        return v.value, nt.value, nr.value
+
+    def excavation(self, ctl: Control, s0_type: int, z0: float, s0: float, k0: float, excavid: Sequence[int],
+                   nexcavid: Optional[Sequence[int]] = None, ninc: int = 1, srf: float = 1.0):
+        excavid = np.ascontiguousarray(excavid, np.int32)
+        nexcavid = np.ones(len(excavid), np.int32) if nexcavid is None else np.ascontiguousarray(nexcavid, np.int32)
+        res = np.zeros(8 * len(nexcavid))
+        n = C.c_int(0)
+        st = lib().sg_excavation(self.h, C.byref(ctl), s0_type, z0, s0, k0, len(nexcavid), _ptr(nexcavid),
+                                 _ptr(excavid), ninc, srf, _ptr(res), C.byref(n))
+        if st:
+            raise SgError(st, self.ctx.last_error)
+        return res.reshape(-1, 8)[: n.value]

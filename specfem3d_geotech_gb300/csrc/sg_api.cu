@@ -1,0 +1,1230 @@
+// sg_api.cu -- C ABI of the solve path (include/sg_solver.h): contexts and
+// device memory, the pcg_solver drop-in, the device-resident model, the
+// slope3d trial / sweep / factor-of-safety drivers and excavation3d.
+//
+// Host code here only orchestrates: every vector operation, reduction and
+// element computation of the solve runs in the kernels of sg_kernels.cu.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "sg_kernels.cuh"
+
+using namespace sg;
+
+namespace {
+
+constexpr double PI_D = 3.141592653589793;
+constexpr double DEG2RAD = PI_D / 180.0, RAD2DEG = 180.0 / PI_D;
+constexpr double INFTOL = 1.0e32, ZEROTOL = 1.0e-12;
+int g_create_status = SG_OK;
+
+void set_tag(char* errtag, const std::string& msg) {
+  if (!errtag) return;
+  size_t n = std::min(msg.size(), (size_t)SG_ERRTAG_LEN);
+  std::memcpy(errtag, msg.data(), n);
+  std::memset(errtag + n, ' ', SG_ERRTAG_LEN - n);  // Fortran blank padding
+}
+
+int next_pow2(int k) {
+  int r = 1;
+  while (r < k) r <<= 1;
+  return r;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct sg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  size_t budget = 0, used = 0;
+  std::unordered_map<void*, size_t> live;
+  std::string err;
+  Profile prof;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+  std::vector<std::pair<int, int>> ev_used;  // (pool index, category)
+  double* pin = nullptr;                     // pinned scratch for scalars
+  int* d_nbr = nullptr;
+  int* d_entry = nullptr;
+  // drop-in cache: the reference calls pcg_solver with the same dof map every
+  // plastic iteration, so the gather topology is rebuilt only when it changes.
+  struct DropIn {
+    std::vector<int> ge;
+    int neq = -1, nelmt = -1;
+    GatherTopo T;
+    int* d_ge = nullptr;
+    double* d_K = nullptr;
+    size_t kcap = 0;
+    double *u = nullptr, *f = nullptr, *dp = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *kp = nullptr,
+           *Y = nullptr, *part = nullptr;
+    int n1cap = 0, necap = 0;
+    ColState* cs = nullptr;
+    PcgGlobal* G = nullptr;
+  } dropin;
+
+  bool check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return true;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return false;
+  }
+  template <typename T>
+  T* alloc(size_t n) {
+    size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    if (budget && used + bytes > budget) { err = "HBM budget exceeded"; return nullptr; }
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) { cudaGetLastError(); err = "cudaMalloc failed"; return nullptr; }
+    used += bytes;
+    live[p] = bytes;
+    return (T*)p;
+  }
+  void release(void* p) {
+    if (!p) return;
+    auto it = live.find(p);
+    if (it != live.end()) { used -= it->second; live.erase(it); }
+    cudaFree(p);
+  }
+  // profiling: events bracket the launches of one category
+  int prof_begin() {
+    if (!prof.on) return -1;
+    size_t idx = ev_used.size();
+    if (idx >= ev_pool.size()) {
+      cudaEvent_t a, b;
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      ev_pool.push_back({a, b});
+    }
+    cudaEventRecord(ev_pool[idx].first, stream);
+    return (int)idx;
+  }
+  void prof_end(int idx, int cat) {
+    if (idx < 0) return;
+    cudaEventRecord(ev_pool[idx].second, stream);
+    ev_used.push_back({idx, cat});
+    prof.counts[1]++;
+    if (cat == 1) prof.counts[0]++;
+    if (ev_used.size() > 4000) prof_flush();
+  }
+  void prof_flush() {
+    if (ev_used.empty()) return;
+    cudaStreamSynchronize(stream);
+    for (auto& u : ev_used) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev_pool[u.first].first, ev_pool[u.first].second);
+      prof.ms[u.second] += ms;
+    }
+    ev_used.clear();
+  }
+};
+
+// ---------------------------------------------------------------------------
+// PCG driver: kp = K u, r = f - kp, z = D r, p = z, then chunks of fused
+// iterations (apply with on-the-fly direction, gather + alpha, update + stop
+// test) until every active column stops.  Between chunks the host reads the
+// device control word; iterations after a column stops are skipped on device.
+// ---------------------------------------------------------------------------
+struct Op {
+  int dense = 0;
+  const void* K = nullptr;
+  const int* ge = nullptr;
+  int nelmt = 0;
+  const GatherTopo* T = nullptr;
+};
+
+template <typename V>
+struct PcgBufs {
+  V *r = nullptr, *z = nullptr, *p = nullptr, *kp = nullptr, *Y = nullptr;
+  double* part = nullptr;
+  ColState* cs = nullptr;
+  PcgGlobal* G = nullptr;
+};
+
+template <typename V, int KR>
+static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u, const V* f, const V* dp, int kcols,
+                     const int* active, int maxiter, double tol, int mode, int* iters, int* failed, int* used_iters) {
+  cudaStream_t s = C->stream;
+  ColState hcs[16];
+  std::memset(hcs, 0, sizeof(hcs));
+  for (int j = 0; j < KR; ++j) {
+    hcs[j].tol = tol;
+    hcs[j].active = (j < kcols && active[j]) ? 1 : 0;
+  }
+  PcgGlobal hg;
+  std::memset(&hg, 0, sizeof(hg));
+  hg.maxiter = maxiter;
+  hg.mode = mode;
+  hg.kcols = kcols;
+  cudaMemcpyAsync(B.cs, hcs, sizeof(ColState) * KR, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(B.G, &hg, sizeof(hg), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(B.p, 0, sizeof(V) * (size_t)n1 * KR, s);
+  cudaMemsetAsync(B.kp, 0, sizeof(V) * (size_t)n1 * KR, s);
+  int ev = C->prof_begin();
+  pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, u, (const V*)nullptr, 0, B.Y, B.cs, B.G, C->d_nbr, s);
+  C->prof_end(ev, 1);
+  ev = C->prof_begin();
+  pcg_gather<V, KR>(*op.T, B.Y, B.kp, B.p, B.z, 0, B.cs, B.G, B.part, s);
+  pcg_update<V, KR>(n1, u, B.r, B.z, B.p, B.kp, f, dp, 1, B.cs, B.G, B.part, s);
+  C->prof_end(ev, 3);
+  const int chunk = op.nelmt >= 50000 ? 4 : (op.nelmt >= 5000 ? 16 : 64);
+  const auto t0 = std::chrono::steady_clock::now();
+  int it = 0;
+  int status = SG_OK;
+  volatile PcgGlobal* hG = (volatile PcgGlobal*)C->pin;
+  while (true) {
+    for (int c = 0; c < chunk; ++c) {
+      ev = C->prof_begin();
+      pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, B.p, B.z, 1, B.Y, B.cs, B.G, C->d_nbr, s);
+      C->prof_end(ev, 1);
+      ev = C->prof_begin();
+      pcg_gather<V, KR>(*op.T, B.Y, B.kp, B.p, B.z, 1, B.cs, B.G, B.part, s);
+      C->prof_end(ev, 2);
+      ev = C->prof_begin();
+      pcg_update<V, KR>(n1, u, B.r, B.z, B.p, B.kp, f, dp, 0, B.cs, B.G, B.part, s);
+      C->prof_end(ev, 3);
+    }
+    cudaMemcpyAsync((void*)hG, B.G, sizeof(PcgGlobal), cudaMemcpyDeviceToHost, s);
+    if (!C->check(cudaStreamSynchronize(s), "pcg")) return SG_ERR_CUDA;
+    it = hG->it;
+    if (hG->all_done) break;
+    if (it >= maxiter + chunk) { status = SG_ERR_TIMEOUT; break; }
+    double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el > 3600.0) { status = SG_ERR_TIMEOUT; C->err = "PCG wall-clock guard"; break; }
+  }
+  cudaMemcpy(hcs, B.cs, sizeof(ColState) * KR, cudaMemcpyDeviceToHost);
+  for (int j = 0; j < kcols; ++j) {
+    iters[j] = hcs[j].iters;
+    failed[j] = hcs[j].failed;
+    if (hcs[j].active && hcs[j].failed && status == SG_OK) status = SG_ERR_NOCONV;
+  }
+  if (used_iters) *used_iters = it;
+  C->prof.counts[2] += it;
+  return status;
+}
+
+template <typename V>
+static int pcg_run(sg_ctx* C, int KR, const Op& op, const PcgBufs<V>& B, int n1, V* u, const V* f, const V* dp,
+                   int kcols, const int* active, int maxiter, double tol, int mode, int* iters, int* failed,
+                   int* used) {
+  switch (KR) {
+    case 1: return pcg_run_t<V, 1>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
+    case 2: return pcg_run_t<V, 2>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
+    case 4: return pcg_run_t<V, 4>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
+    case 8: return pcg_run_t<V, 8>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
+    case 16: return pcg_run_t<V, 16>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
+  }
+  return SG_ERR_BADARG;
+}
+
+// Element-apply of K (sparse layout, KR columns) followed by the plain gather:
+// out = K x.  Used for warm-start products and FP64 refinement residuals.
+template <typename V>
+static void apply_plain(sg_ctx* C, int KR, const Op& op, const V* x, V* Y, V* out) {
+  int ev = C->prof_begin();
+  switch (KR) {
+    case 1: pcg_apply<V, 1>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
+    case 2: pcg_apply<V, 2>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
+    case 4: pcg_apply<V, 4>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
+    case 8: pcg_apply<V, 8>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
+    case 16: pcg_apply<V, 16>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
+  }
+  C->prof_end(ev, 1);
+  ev = C->prof_begin();
+  launch_gather_plain<V>(*op.T, KR, Y, out, 0, nullptr, C->stream);
+  C->prof_end(ev, 2);
+}
+
+// ---------------------------------------------------------------------------
+extern "C" {
+
+sg_ctx* sg_create(int device, size_t hbm_budget) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
+    cudaGetLastError();
+    g_create_status = SG_ERR_NODEVICE;
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) { g_create_status = SG_ERR_NODEVICE; return nullptr; }
+  sg_ctx* c = new sg_ctx();
+  c->device = device;
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  c->budget = hbm_budget ? hbm_budget : fr;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    g_create_status = SG_ERR_CUDA;
+    return nullptr;
+  }
+  cudaMallocHost((void**)&c->pin, 4096);
+  upload_constants();
+  const KsTables& T = ks_tables();
+  c->d_nbr = c->alloc<int>(NGLL * KS_NBR);
+  c->d_entry = c->alloc<int>(KS_NNZ);
+  cudaMemcpy(c->d_nbr, T.nbr, sizeof(T.nbr), cudaMemcpyHostToDevice);
+  cudaMemcpy(c->d_entry, T.entry, sizeof(T.entry), cudaMemcpyHostToDevice);
+  if (cudaGetLastError() != cudaSuccess) {
+    g_create_status = SG_ERR_NODEVICE;
+    delete c;
+    return nullptr;
+  }
+  g_create_status = SG_OK;
+  return c;
+}
+
+int sg_create_status(void) { return g_create_status; }
+
+static void free_topo(sg_ctx* c, GatherTopo& T) {
+  c->release(T.d_ptr); c->release(T.d_ent); c->release(T.d_dof);
+  T.d_ptr = T.d_ent = T.d_dof = nullptr;
+}
+
+static bool upload_topo(sg_ctx* c, GatherTopo& T) {
+  free_topo(c, T);
+  T.d_ptr = c->alloc<int>(T.ptr.size());
+  T.d_ent = c->alloc<int>(T.ent.size());
+  T.d_dof = c->alloc<int>(T.dof.size());
+  if (!T.d_ptr || !T.d_ent || !T.d_dof) return false;
+  cudaMemcpyAsync(T.d_ptr, T.ptr.data(), sizeof(int) * T.ptr.size(), cudaMemcpyHostToDevice, c->stream);
+  if (!T.ent.empty()) cudaMemcpyAsync(T.d_ent, T.ent.data(), sizeof(int) * T.ent.size(), cudaMemcpyHostToDevice, c->stream);
+  if (!T.dof.empty()) cudaMemcpyAsync(T.d_dof, T.dof.data(), sizeof(int) * T.dof.size(), cudaMemcpyHostToDevice, c->stream);
+  return true;
+}
+
+void sg_destroy(sg_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->live) cudaFree(kv.first);
+  c->live.clear();
+  for (auto& e : c->ev_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  if (c->pin) cudaFreeHost(c->pin);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* sg_last_error(const sg_ctx* c) { return c ? c->err.c_str() : "no context"; }
+size_t sg_hbm_used(const sg_ctx* c) { return c ? c->used : 0; }
+
+int sg_profile_enable(sg_ctx* c, int on) {
+  if (!c) return SG_ERR_BADARG;
+  c->prof_flush();
+  c->prof = Profile();
+  c->prof.on = on != 0;
+  return SG_OK;
+}
+
+int sg_profile_read(sg_ctx* c, double* ms, long long* counts) {
+  if (!c) return SG_ERR_BADARG;
+  c->prof_flush();
+  for (int i = 0; i < 8; ++i) ms[i] = c->prof.ms[i];
+  for (int i = 0; i < 4; ++i) counts[i] = c->prof.counts[i];
+  return SG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The drop-in: pcg_solver (src/solver.f90:14-79)
+// ---------------------------------------------------------------------------
+int sg_pcg_solve(sg_ctx* c, int neq, int nelmt, int nedof, const double* k, double* u, const double* f,
+                 const double* dprecon, const int* gdof_elmt, int cg_maxiter, double cg_tol, int* cg_iter,
+                 char* errtag) {
+  set_tag(errtag, "ERROR: unknown!");
+  if (!c) return SG_ERR_BADARG;
+  if (nedof != NEDOF || neq < 0 || nelmt < 0 || !k || !u || !f || !dprecon || !gdof_elmt || !cg_iter) {
+    set_tag(errtag, "ERROR: bad argument to sg_pcg_solve (nedof must be 81)!");
+    return SG_ERR_BADARG;
+  }
+  for (size_t i = 0; i < (size_t)nelmt * NEDOF; ++i)
+    if (gdof_elmt[i] < 0 || gdof_elmt[i] > neq) {
+      set_tag(errtag, "ERROR: gdof_elmt entry out of [0,neq]!");
+      return SG_ERR_BADARG;
+    }
+  cudaSetDevice(c->device);
+  auto& D = c->dropin;
+  const int n1 = neq + 1;
+  const size_t nk = (size_t)nelmt * NEDOF * NEDOF;
+  bool same_map = (D.neq == neq && D.nelmt == nelmt &&
+                   std::memcmp(D.ge.data(), gdof_elmt, sizeof(int) * (size_t)nelmt * NEDOF) == 0);
+  if (!same_map) {
+    D.ge.assign(gdof_elmt, gdof_elmt + (size_t)nelmt * NEDOF);
+    build_groups_from_gdof(gdof_elmt, nelmt, neq, D.T);
+    if (!upload_topo(c, D.T)) { set_tag(errtag, "ERROR: out of device memory!"); return SG_ERR_OOM; }
+    D.neq = neq;
+    D.nelmt = nelmt;
+  }
+  if (D.kcap < nk || D.necap < nelmt) {
+    c->release(D.d_K); c->release(D.d_ge); c->release(D.Y);
+    D.d_K = c->alloc<double>(nk);
+    D.d_ge = c->alloc<int>((size_t)nelmt * NEDOF);
+    D.Y = c->alloc<double>((size_t)nelmt * NEDOF);
+    D.kcap = nk;
+    D.necap = nelmt;
+  }
+  if (D.n1cap < n1) {
+    for (double* p : {D.u, D.f, D.dp, D.r, D.z, D.p, D.kp}) c->release(p);
+    D.u = c->alloc<double>(n1); D.f = c->alloc<double>(n1); D.dp = c->alloc<double>(n1);
+    D.r = c->alloc<double>(n1); D.z = c->alloc<double>(n1); D.p = c->alloc<double>(n1); D.kp = c->alloc<double>(n1);
+    D.n1cap = n1;
+  }
+  if (!D.part) {
+    D.part = c->alloc<double>((size_t)NPART * 16 * 4);
+    D.cs = c->alloc<ColState>(16);
+    D.G = c->alloc<PcgGlobal>(1);
+  }
+  if (!D.d_K || !D.d_ge || !D.Y || !D.u || !D.part || !D.cs || !D.G) {
+    set_tag(errtag, "ERROR: out of device memory!");
+    return SG_ERR_OOM;
+  }
+  cudaStream_t s = c->stream;
+  cudaMemcpyAsync(D.d_K, k, sizeof(double) * nk, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(D.d_ge, gdof_elmt, sizeof(int) * (size_t)nelmt * NEDOF, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(D.u, u, sizeof(double) * n1, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(D.f, f, sizeof(double) * n1, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(D.dp, dprecon, sizeof(double) * n1, cudaMemcpyHostToDevice, s);
+  Op op;
+  op.dense = 1; op.K = D.d_K; op.ge = D.d_ge; op.nelmt = nelmt; op.T = &D.T;
+  PcgBufs<double> B;
+  B.r = D.r; B.z = D.z; B.p = D.p; B.kp = D.kp; B.Y = D.Y; B.part = D.part; B.cs = D.cs; B.G = D.G;
+  int active = 1, it = 0, failed = 0;
+  int st = pcg_run_t<double, 1>(c, op, B, n1, D.u, D.f, D.dp, 1, &active, cg_maxiter, cg_tol, 0, &it, &failed,
+                                nullptr);
+  cudaMemcpyAsync(u, D.u, sizeof(double) * n1, cudaMemcpyDeviceToHost, s);
+  if (!c->check(cudaStreamSynchronize(s), "sg_pcg_solve")) {
+    set_tag(errtag, "ERROR: CUDA failure: " + c->err);
+    return SG_ERR_CUDA;
+  }
+  *cg_iter = it;
+  if (st == SG_ERR_NOCONV) {
+    set_tag(errtag, "ERROR: PCG solver doesn't converge!");
+    return SG_ERR_NOCONV;
+  }
+  if (st != SG_OK) {
+    set_tag(errtag, "ERROR: " + c->err);
+    return st;
+  }
+  set_tag(errtag, "");
+  return SG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// device-resident model
+// ---------------------------------------------------------------------------
+struct TrialWork {
+  int KR = 0, n1 = 0, nel = 0;
+  double *x = nullptr, *oldx = nullptr, *load = nullptr, *bodyload = nullptr, *Yb = nullptr;
+  double *evpt = nullptr, *stress = nullptr;  // KR * nelmt_all * 27 * 6
+  MatF* mf = nullptr;                          // KR * nmatblk
+  PcgBufs<double> b64;
+  PcgBufs<float> b32;
+  // mixed form
+  double *kp64 = nullptr, *r64 = nullptr;
+  float *r32 = nullptr, *d32 = nullptr;
+  int* colmask = nullptr;
+  double* red = nullptr;
+};
+
+struct sg_model {
+  sg_ctx* ctx = nullptr;
+  HostMesh H;
+  int precision = SG_PREC_FP64;
+  double* d_coord = nullptr;
+  int *d_gnum = nullptr, *d_matid = nullptr, *d_ge = nullptr, *d_gdof = nullptr;
+  double *d_ym = nullptr, *d_nu = nullptr, *d_gam = nullptr;
+  double* d_geo = nullptr;
+  GatherTopo T;
+  double* d_K64 = nullptr;
+  float* d_K32 = nullptr;
+  double *d_diag = nullptr, *d_dprecon = nullptr, *d_extload = nullptr;
+  float* d_dprecon32 = nullptr;
+  double* d_Yscratch = nullptr;  // nelmt*81 (diag / gravity element vectors)
+  TrialWork W;
+  std::vector<double> last_stress_ok;
+  double* d_fpart = nullptr;
+};
+
+static void model_release_work(sg_model* M) {
+  sg_ctx* c = M->ctx;
+  TrialWork& W = M->W;
+  for (void* p : {(void*)W.x, (void*)W.oldx, (void*)W.load, (void*)W.bodyload, (void*)W.Yb, (void*)W.evpt,
+                  (void*)W.stress, (void*)W.mf, (void*)W.b64.r, (void*)W.b64.z, (void*)W.b64.p, (void*)W.b64.kp,
+                  (void*)W.b64.Y, (void*)W.b64.part, (void*)W.b64.cs, (void*)W.b64.G, (void*)W.b32.r, (void*)W.b32.z,
+                  (void*)W.b32.p, (void*)W.b32.kp, (void*)W.b32.Y, (void*)W.kp64, (void*)W.r64, (void*)W.r32,
+                  (void*)W.d32, (void*)W.colmask, (void*)W.red})
+    c->release(p);
+  W = TrialWork();
+}
+
+// Allocate the per-batch workspace for KR columns (n1 dofs, nel operator elements).
+static bool model_work(sg_model* M, int KR, int n1, int nel) {
+  TrialWork& W = M->W;
+  if (W.KR == KR && W.n1 == n1 && W.nel == nel) return true;
+  model_release_work(M);
+  sg_ctx* c = M->ctx;
+  const size_t nv = (size_t)n1 * KR, ny = (size_t)nel * NEDOF * KR;
+  const size_t ns = (size_t)KR * M->H.nelmt * NGLL * NST;
+  W.KR = KR; W.n1 = n1; W.nel = nel;
+  W.x = c->alloc<double>(nv); W.oldx = c->alloc<double>(nv); W.load = c->alloc<double>(nv);
+  W.bodyload = c->alloc<double>(nv); W.Yb = c->alloc<double>(ny);
+  W.evpt = c->alloc<double>(ns); W.stress = c->alloc<double>(ns);
+  W.mf = c->alloc<MatF>((size_t)KR * M->H.nmatblk);
+  W.b64.part = c->alloc<double>((size_t)NPART * 16 * 4);
+  W.b64.cs = c->alloc<ColState>(16);
+  W.b64.G = c->alloc<PcgGlobal>(1);
+  W.red = c->alloc<double>(64);
+  W.colmask = c->alloc<int>(16);
+  bool ok = W.x && W.oldx && W.load && W.bodyload && W.Yb && W.evpt && W.stress && W.mf && W.b64.part && W.b64.cs &&
+            W.b64.G && W.red && W.colmask;
+  if (M->precision == SG_PREC_FP64) {
+    W.b64.r = c->alloc<double>(nv); W.b64.z = c->alloc<double>(nv); W.b64.p = c->alloc<double>(nv);
+    W.b64.kp = c->alloc<double>(nv); W.b64.Y = W.Yb;  // the apply and body-load gathers share Y
+    ok = ok && W.b64.r && W.b64.z && W.b64.p && W.b64.kp;
+  } else {
+    W.b32.r = c->alloc<float>(nv); W.b32.z = c->alloc<float>(nv); W.b32.p = c->alloc<float>(nv);
+    W.b32.kp = c->alloc<float>(nv); W.b32.Y = c->alloc<float>(ny);
+    W.b32.part = W.b64.part; W.b32.cs = W.b64.cs; W.b32.G = W.b64.G;
+    W.kp64 = c->alloc<double>(nv); W.r64 = c->alloc<double>(nv); W.r32 = c->alloc<float>(nv); W.d32 = c->alloc<float>(nv);
+    W.b64.Y = W.Yb;
+    ok = ok && W.b32.r && W.b32.z && W.b32.p && W.b32.kp && W.b32.Y && W.kp64 && W.r64 && W.r32 && W.d32;
+  }
+  if (!ok) model_release_work(M);
+  return ok;
+}
+
+// Builds K, the diagonal preconditioner and the gravity load for the
+// element list (all elements when elist is null) with Poisson ratios nuv.
+static bool model_stiffness(sg_model* M, const int* d_elist, int nel, const double* d_nuv, const GatherTopo& T,
+                            const int* d_ge_local, int n1, bool gravity) {
+  sg_ctx* c = M->ctx;
+  cudaStream_t s = c->stream;
+  double* Ydiag = M->d_Yscratch;
+  double* Ygrav = M->d_Yscratch + (size_t)M->H.nelmt * NEDOF;
+  int ev = c->prof_begin();
+  launch_stiffness(M->d_geo, M->d_matid, d_elist, nel, M->d_ym, d_nuv, M->d_gam, M->d_K64, M->d_K32, Ydiag,
+                   gravity ? Ygrav : nullptr, c->d_entry, s);
+  c->prof_end(ev, 5);
+  cudaMemsetAsync(M->d_diag, 0, sizeof(double) * n1, s);
+  launch_gather_plain<double>(T, 1, Ydiag, M->d_diag, 0, nullptr, s);
+  cudaMemcpyAsync(M->d_dprecon, M->d_diag, sizeof(double) * n1, cudaMemcpyDeviceToDevice, s);
+  launch_invert_diag(n1, M->d_dprecon, M->d_dprecon32, s);
+  if (gravity) {
+    cudaMemsetAsync(M->d_extload, 0, sizeof(double) * n1, s);
+    launch_gather_plain<double>(T, 1, Ygrav, M->d_extload, 0, nullptr, s);
+  }
+  (void)d_ge_local;
+  return c->check(cudaGetLastError(), "stiffness");
+}
+
+extern "C" {
+
+static sg_model* model_build(sg_ctx* c, HostMesh&& H, int nnode8, const double* x8, const double* y8,
+                             const double* z8, const int* conn8, const int* bc_counts, const int* bc_pairs,
+                             int precision, char* errtag) {
+  std::string err;
+  cudaSetDevice(c->device);
+  sg_model* M = new sg_model();
+  M->ctx = c;
+  M->precision = precision;
+  M->H = std::move(H);
+  HostMesh& h = M->H;
+  if (!hex2spec(h, nnode8, x8, y8, z8, conn8, err) || !apply_bc(h, bc_counts, bc_pairs, err)) {
+    set_tag(errtag, err);
+    delete M;
+    return nullptr;
+  }
+  build_gdof_elmt(h);
+  build_groups_from_gdof(h.gdof_elmt.data(), h.nelmt, h.neq, M->T);
+  cudaStream_t s = c->stream;
+  const int ne = h.nelmt, n1 = h.neq + 1;
+  M->d_coord = c->alloc<double>(h.g_coord.size());
+  M->d_gnum = c->alloc<int>(h.g_num.size());
+  M->d_matid = c->alloc<int>(ne);
+  M->d_ge = c->alloc<int>(h.gdof_elmt.size());
+  M->d_gdof = c->alloc<int>(h.gdof.size());
+  M->d_ym = c->alloc<double>(h.nmatblk);
+  M->d_nu = c->alloc<double>(h.nmatblk);
+  M->d_gam = c->alloc<double>(h.nmatblk);
+  M->d_geo = c->alloc<double>((size_t)ne * NGLL * GEO_STRIDE);
+  M->d_K64 = c->alloc<double>((size_t)ne * KS_STRIDE);
+  if (precision == SG_PREC_MIXED) {
+    M->d_K32 = c->alloc<float>((size_t)ne * KS_STRIDE);
+    M->d_dprecon32 = c->alloc<float>(n1);
+  }
+  M->d_diag = c->alloc<double>(n1);
+  M->d_dprecon = c->alloc<double>(n1);
+  M->d_extload = c->alloc<double>(n1);
+  M->d_Yscratch = c->alloc<double>((size_t)2 * ne * NEDOF);
+  M->d_fpart = c->alloc<double>(NPART * 2);
+  bool ok = M->d_coord && M->d_gnum && M->d_matid && M->d_ge && M->d_gdof && M->d_ym && M->d_nu && M->d_gam &&
+            M->d_geo && M->d_K64 && M->d_diag && M->d_dprecon && M->d_extload && M->d_Yscratch && M->d_fpart &&
+            (precision == SG_PREC_FP64 || (M->d_K32 && M->d_dprecon32)) && upload_topo(c, M->T);
+  if (!ok) {
+    set_tag(errtag, "ERROR: the model does not fit the device memory budget!");
+    sg_model_free(M);
+    return nullptr;
+  }
+  cudaMemcpyAsync(M->d_coord, h.g_coord.data(), sizeof(double) * h.g_coord.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(M->d_gnum, h.g_num.data(), sizeof(int) * h.g_num.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(M->d_matid, h.mat_id.data(), sizeof(int) * ne, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(M->d_ge, h.gdof_elmt.data(), sizeof(int) * h.gdof_elmt.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(M->d_gdof, h.gdof.data(), sizeof(int) * h.gdof.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(M->d_ym, h.ym.data(), sizeof(double) * h.nmatblk, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(M->d_nu, h.nu.data(), sizeof(double) * h.nmatblk, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(M->d_gam, h.gam.data(), sizeof(double) * h.nmatblk, cudaMemcpyHostToDevice, s);
+  launch_geometry(M->d_coord, M->d_gnum, ne, M->d_geo, s);
+  model_stiffness(M, nullptr, ne, M->d_nu, M->T, M->d_ge, n1, true);
+  if (!c->check(cudaStreamSynchronize(s), "model build")) {
+    set_tag(errtag, "ERROR: CUDA failure: " + c->err);
+    sg_model_free(M);
+    return nullptr;
+  }
+  set_tag(errtag, "");
+  return M;
+}
+
+sg_model* sg_model_from_hex8(sg_ctx* c, int nnode8, const double* x8, const double* y8, const double* z8, int nelmt,
+                             const int* conn8, const int* mat_id, int nmatblk, const double* props,
+                             const int* bc_counts, const int* bc_pairs, int precision, char* errtag) {
+  set_tag(errtag, "ERROR: unknown!");
+  if (!c || nnode8 <= 0 || nelmt <= 0 || nmatblk <= 0 || !x8 || !y8 || !z8 || !conn8 || !mat_id || !props ||
+      !bc_counts || (precision != SG_PREC_FP64 && precision != SG_PREC_MIXED)) {
+    set_tag(errtag, "ERROR: bad argument to sg_model_from_hex8!");
+    return nullptr;
+  }
+  HostMesh H;
+  H.nelmt = nelmt;
+  H.nmatblk = nmatblk;
+  H.mat_id.assign(mat_id, mat_id + nelmt);
+  for (int m : H.mat_id)
+    if (m < 1 || m > nmatblk) {
+      set_tag(errtag, "ERROR: material IDs must be consistent with the defined material regions!");
+      return nullptr;
+    }
+  for (int i = 0; i < nmatblk; ++i) {
+    H.gam.push_back(props[6 * i + 0]); H.ym.push_back(props[6 * i + 1]); H.nu.push_back(props[6 * i + 2]);
+    H.phi.push_back(props[6 * i + 3]); H.coh.push_back(props[6 * i + 4]); H.psi.push_back(props[6 * i + 5]);
+  }
+  H.srf.assign(1, 1.0);
+  return model_build(c, std::move(H), nnode8, x8, y8, z8, conn8, bc_counts, bc_pairs, precision, errtag);
+}
+
+sg_model* sg_model_from_deck(sg_ctx* c, const char* path, int precision, char* errtag) {
+  set_tag(errtag, "ERROR: unknown!");
+  if (!c || !path) return nullptr;
+  HostMesh H;
+  std::vector<double> x8, y8, z8, props;
+  std::vector<int> conn, mid, cnt, pairs;
+  std::string err;
+  if (!read_deck(path, H, x8, y8, z8, conn, mid, props, cnt, pairs, err)) {
+    set_tag(errtag, err);
+    return nullptr;
+  }
+  H.mat_id = mid;
+  for (int i = 0; i < H.nmatblk; ++i) {
+    H.gam.push_back(props[6 * i + 0]); H.ym.push_back(props[6 * i + 1]); H.nu.push_back(props[6 * i + 2]);
+    H.phi.push_back(props[6 * i + 3]); H.coh.push_back(props[6 * i + 4]); H.psi.push_back(props[6 * i + 5]);
+  }
+  return model_build(c, std::move(H), (int)x8.size(), x8.data(), y8.data(), z8.data(), conn.data(), cnt.data(),
+                     pairs.data(), precision, errtag);
+}
+
+void sg_model_free(sg_model* M) {
+  if (!M) return;
+  sg_ctx* c = M->ctx;
+  cudaStreamSynchronize(c->stream);
+  model_release_work(M);
+  free_topo(c, M->T);
+  for (void* p : {(void*)M->d_coord, (void*)M->d_gnum, (void*)M->d_matid, (void*)M->d_ge, (void*)M->d_gdof,
+                  (void*)M->d_ym, (void*)M->d_nu, (void*)M->d_gam, (void*)M->d_geo, (void*)M->d_K64, (void*)M->d_K32,
+                  (void*)M->d_diag, (void*)M->d_dprecon, (void*)M->d_extload, (void*)M->d_dprecon32,
+                  (void*)M->d_Yscratch, (void*)M->d_fpart})
+    c->release(p);
+  delete M;
+}
+
+int sg_model_info(const sg_model* M, int* info) {
+  if (!M || !info) return SG_ERR_BADARG;
+  info[0] = M->H.nnode; info[1] = M->H.nelmt; info[2] = M->H.neq; info[3] = M->H.nmatblk;
+  info[4] = (int)M->H.srf.size(); info[5] = M->T.ngroups; info[6] = 0; info[7] = 0;
+  return SG_OK;
+}
+
+int sg_model_arrays(const sg_model* M, double* g_coord, int* g_num, int* gdof, int* gdof_elmt) {
+  if (!M) return SG_ERR_BADARG;
+  const HostMesh& h = M->H;
+  if (g_coord) std::memcpy(g_coord, h.g_coord.data(), sizeof(double) * h.g_coord.size());
+  if (g_num) std::memcpy(g_num, h.g_num.data(), sizeof(int) * h.g_num.size());
+  if (gdof) std::memcpy(gdof, h.gdof.data(), sizeof(int) * h.gdof.size());
+  if (gdof_elmt) std::memcpy(gdof_elmt, h.gdof_elmt.data(), sizeof(int) * h.gdof_elmt.size());
+  return SG_OK;
+}
+
+int sg_model_control(const sg_model* M, double* dctl, int* ictl, double* srf) {
+  if (!M) return SG_ERR_BADARG;
+  const HostMesh& h = M->H;
+  if (dctl) { dctl[0] = h.cg_tol; dctl[1] = h.nl_tol; }
+  if (ictl) { ictl[0] = h.cg_maxiter; ictl[1] = h.nl_maxiter; ictl[2] = h.phinu; ictl[3] = h.allelastic; ictl[4] = h.nexcav; ictl[5] = h.ninc; }
+  if (srf) std::memcpy(srf, h.srf.data(), sizeof(double) * h.srf.size());
+  return SG_OK;
+}
+
+int sg_model_stiffness(sg_model* M, double* storekm, double* dprecon, double* extload) {
+  if (!M) return SG_ERR_BADARG;
+  sg_ctx* c = M->ctx;
+  cudaSetDevice(c->device);
+  const int ne = M->H.nelmt, n1 = M->H.neq + 1;
+  if (storekm) {
+    double* dense = c->alloc<double>((size_t)ne * NEDOF * NEDOF);
+    if (!dense) return SG_ERR_OOM;
+    launch_expand_dense(M->d_K64, ne, dense, c->d_entry, c->stream);
+    cudaMemcpyAsync(storekm, dense, sizeof(double) * ne * NEDOF * NEDOF, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    c->release(dense);
+  }
+  if (dprecon) cudaMemcpyAsync(dprecon, M->d_diag, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream);
+  if (extload) cudaMemcpyAsync(extload, M->d_extload, sizeof(double) * n1, cudaMemcpyDeviceToHost, c->stream);
+  return c->check(cudaStreamSynchronize(c->stream), "stiffness export") ? SG_OK : SG_ERR_CUDA;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// strength reduction and pseudo-time step (host, per trial; FP64)
+// ---------------------------------------------------------------------------
+// strength_reduction (src/plastic_library.f90:42-88); returns istat.
+static int strength_reduction(const HostMesh& h, double srf, bool phinu, std::vector<double>& cohf,
+                              std::vector<double>& nuf, std::vector<double>& phif, std::vector<double>& psif) {
+  const int nm = h.nmatblk;
+  cohf = h.coh; nuf = h.nu; phif = h.phi; psif = h.psi;
+  int istat = 0;
+  if (srf != 1.0)
+    for (int i = 0; i < nm; ++i) {
+      phif[i] = std::atan(std::tan(h.phi[i] * DEG2RAD) / srf) * RAD2DEG;
+      psif[i] = std::atan(std::tan(h.psi[i] * DEG2RAD) / srf) * RAD2DEG;
+      cohf[i] = h.coh[i] / srf;
+    }
+  if (!phinu) return istat;
+  for (int i = 0; i < nm; ++i) {
+    double omtnu = 1.0 - 2.0 * h.nu[i];
+    double snphif = std::sin(phif[i] * DEG2RAD);
+    if (snphif < omtnu) {
+      double beta = std::sin(h.phi[i] * DEG2RAD) / omtnu;
+      if (beta < 1.0) beta = 1.0 + ZEROTOL;
+      nuf[i] = 0.5 * (1.0 - snphif / beta);
+      istat = 1;
+    }
+  }
+  return istat;
+}
+
+// dt_viscoplas (src/plastic_library.f90:17-39)
+static double dt_viscoplas(const std::vector<double>& nuf, const std::vector<double>& phif,
+                           const std::vector<double>& ym, const std::vector<char>* ismat) {
+  double dtm = INFTOL;
+  for (size_t i = 0; i < nuf.size(); ++i) {
+    if (ismat && !(*ismat)[i]) continue;
+    double sn = std::sin(phif[i] * DEG2RAD);
+    double dt = 4.0 * (1.0 + nuf[i]) * (1.0 - 2.0 * nuf[i]) / (ym[i] * (1.0 - 2.0 * nuf[i] + sn * sn));
+    if (dt < dtm) dtm = dt;
+  }
+  return dtm;
+}
+
+static void make_matf(const HostMesh& h, const std::vector<double>& ymv, const std::vector<double>& nuf,
+                      const std::vector<double>& phif, const std::vector<double>& cohf,
+                      const std::vector<double>& psif, std::vector<MatF>& out) {
+  out.resize(h.nmatblk);
+  for (int i = 0; i < h.nmatblk; ++i) {
+    double E = ymv[i], v = nuf[i];
+    double Ef = E / ((1.0 + v) * (1.0 - 2.0 * v));
+    MatF& m = out[i];
+    m.c11 = (1.0 - v) * Ef; m.c12 = v * Ef; m.c44 = 0.5 * (1.0 - 2.0 * v) * Ef;
+    m.snph = std::sin(phif[i] * DEG2RAD); m.csph = std::cos(phif[i] * DEG2RAD);
+    m.cohf = cohf[i];
+    m.snps = std::sin(psif[i] * DEG2RAD);
+    m.pad = 0;
+  }
+}
+
+// Reads KR*nq reduced values (fixed-order device reduction) to the host.
+static void reduce_read(sg_ctx* c, const double* part, int nblk, int KR, int nq, int maxmask, double* d_out,
+                        double* h_out) {
+  launch_final_reduce(part, nblk, KR, nq, maxmask, d_out, c->stream);
+  cudaMemcpyAsync(c->pin + 256, d_out, sizeof(double) * KR * nq, cudaMemcpyDeviceToHost, c->stream);
+  cudaStreamSynchronize(c->stream);
+  std::memcpy(h_out, c->pin + 256, sizeof(double) * KR * nq);
+}
+
+// ---------------------------------------------------------------------------
+// Linear solve of one plastic iteration for the active columns.
+// FP64: the reference PCG on the FP64 element matrices.
+// MIXED: FP64 iterative refinement -- r = f - K64 x in FP64, an FP32 PCG on
+// the FP32 element matrices solves K d = r to a relative residual
+// inner_rtol, x += d; a column is solved when |f - K x|/|f| <= refine_rtol and
+// its last correction passes the reference step test max|d|/max|x| <= cg_tol.
+// ---------------------------------------------------------------------------
+struct SolveStats {
+  int iters[16];
+  int refine = 0;
+};
+
+static int linear_solve(sg_model* M, const sg_control* ctl, const Op& op64, const Op& op32, int k,
+                        const std::vector<int>& active, SolveStats& S, const double* dprecon, const float* dprecon32) {
+  sg_ctx* c = M->ctx;
+  TrialWork& W = M->W;
+  const int KR = W.KR, n1 = W.n1;
+  for (int j = 0; j < 16; ++j) S.iters[j] = 0;
+  if (M->precision == SG_PREC_FP64) {
+    int it[16], fl[16], used = 0;
+    int st = pcg_run<double>(c, KR, op64, W.b64, n1, W.x, W.load, dprecon, k, active.data(), ctl->cg_maxiter,
+                             ctl->cg_tol, 0, it, fl, &used);
+    for (int j = 0; j < k; ++j) S.iters[j] = active[j] ? it[j] : 0;
+    return st;
+  }
+  const double rtol = ctl->refine_rtol > 0 ? ctl->refine_rtol : 1e-10;
+  const double itol = ctl->inner_rtol > 0 ? ctl->inner_rtol : 1e-4;
+  std::vector<int> live(active);
+  std::vector<int> step_ok(k, 0);
+  double red[64];
+  for (int round = 0; round < 60; ++round) {
+    apply_plain<double>(c, KR, op64, W.x, W.Yb, W.kp64);
+    launch_residual_norms(n1, KR, W.load, W.kp64, W.r64, W.r32, W.b64.part, c->stream);
+    reduce_read(c, W.b64.part, NPART, KR, 2, 0, W.red, red);
+    S.refine++;
+    c->prof.counts[3]++;
+    bool any = false;
+    for (int j = 0; j < k; ++j) {
+      if (!live[j]) continue;
+      double rr = red[2 * j], ff = red[2 * j + 1];
+      bool small = ff > 0 ? std::sqrt(rr / ff) <= rtol : rr == 0.0;
+      if (small && (step_ok[j] || round == 0)) live[j] = 0;
+      else any = true;
+    }
+    if (!any) return SG_OK;
+    // inner FP32 solve K d = r for the live columns
+    cudaMemsetAsync(W.d32, 0, sizeof(float) * (size_t)n1 * KR, c->stream);
+    int it[16], fl[16], used = 0;
+    int st = pcg_run<float>(c, KR, op32, W.b32, n1, W.d32, W.r32, dprecon32, k, live.data(), ctl->cg_maxiter,
+                            itol, 1, it, fl, &used);
+    if (st != SG_OK && st != SG_ERR_NOCONV) return st;
+    int mask[16] = {0};
+    for (int j = 0; j < k; ++j) {
+      mask[j] = live[j];
+      if (live[j]) S.iters[j] += it[j];
+    }
+    cudaMemcpyAsync(W.colmask, mask, sizeof(int) * 16, cudaMemcpyHostToDevice, c->stream);
+    launch_axpy_correction(n1, KR, W.colmask, W.d32, W.x, W.b64.part, c->stream);
+    reduce_read(c, W.b64.part, NPART, KR, 2, 3, W.red, red);
+    for (int j = 0; j < k; ++j)
+      if (live[j]) step_ok[j] = (red[2 * j + 1] > 0) && (red[2 * j] / red[2 * j + 1] <= ctl->cg_tol);
+  }
+  c->err = "iterative refinement did not converge";
+  return SG_ERR_NOCONV;
+}
+
+// ---------------------------------------------------------------------------
+// k concurrent SRF trials of slope3d (src/slope.F90:244-443)
+// ---------------------------------------------------------------------------
+static int run_trials(sg_model* M, const sg_control* ctl, int k, const double* srf, sg_trial_result* res,
+                      double* x_out) {
+  sg_ctx* c = M->ctx;
+  HostMesh& h = M->H;
+  if (k < 1 || k > 16 || !ctl || !srf || !res) return SG_ERR_BADARG;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const int n1 = h.neq + 1, KR = next_pow2(k), ne = h.nelmt;
+  const auto t_start = std::chrono::steady_clock::now();
+  if (!model_work(M, KR, n1, ne)) { c->err = "trial workspace does not fit the HBM budget"; return SG_ERR_OOM; }
+  TrialWork& W = M->W;
+  // per-trial factored properties
+  std::vector<double> dt(k);
+  std::vector<MatF> mf_all((size_t)KR * h.nmatblk);
+  bool restiff = false;
+  std::vector<double> nuf_first;
+  for (int t = 0; t < k; ++t) {
+    std::vector<double> cohf, nuf, phif, psif;
+    int istat = strength_reduction(h, srf[t], ctl->phinu != 0, cohf, nuf, phif, psif);
+    if (istat == 1) {
+      if (k > 1) { c->err = "phi-nu correction changes the stiffness: run such trials one at a time"; return SG_ERR_BADARG; }
+      restiff = true;
+      nuf_first = nuf;
+    }
+    dt[t] = dt_viscoplas(nuf, phif, h.ym, nullptr);
+    std::vector<MatF> mf;
+    make_matf(h, h.ym, nuf, phif, cohf, psif, mf);
+    std::copy(mf.begin(), mf.end(), mf_all.begin() + (size_t)t * h.nmatblk);
+  }
+  cudaMemcpyAsync(W.mf, mf_all.data(), sizeof(MatF) * mf_all.size(), cudaMemcpyHostToDevice, s);
+  double* d_nuf = nullptr;
+  if (restiff) {
+    d_nuf = c->alloc<double>(h.nmatblk);
+    cudaMemcpyAsync(d_nuf, nuf_first.data(), sizeof(double) * h.nmatblk, cudaMemcpyHostToDevice, s);
+    model_stiffness(M, nullptr, ne, d_nuf, M->T, M->d_ge, n1, false);
+  }
+  const size_t nv = (size_t)n1 * KR;
+  const size_t nst = (size_t)ne * NGLL * NST;
+  cudaMemsetAsync(W.x, 0, sizeof(double) * nv, s);
+  cudaMemsetAsync(W.oldx, 0, sizeof(double) * nv, s);
+  cudaMemsetAsync(W.bodyload, 0, sizeof(double) * nv, s);
+  cudaMemsetAsync(W.evpt, 0, sizeof(double) * nst * KR, s);
+  cudaMemsetAsync(W.stress, 0, sizeof(double) * nst * KR, s);
+  Op op64, op32;
+  op64.K = M->d_K64; op64.ge = M->d_ge; op64.nelmt = ne; op64.T = &M->T;
+  op32 = op64;
+  op32.K = M->d_K32;
+  std::vector<int> live(k, 1);
+  std::vector<int> done(k, 0);
+  for (int t = 0; t < k; ++t) {
+    res[t] = sg_trial_result();
+    res[t].srf = srf[t];
+  }
+  int status = SG_OK;
+  double red[64];
+  for (int nl_iter = 1; nl_iter <= ctl->nl_maxiter; ++nl_iter) {
+    bool any = false;
+    for (int t = 0; t < k; ++t) any = any || live[t];
+    if (!any) break;
+    launch_load_combine(n1, KR, M->d_extload, W.bodyload, W.load, s);
+    SolveStats S;
+    int st = linear_solve(M, ctl, op64, op32, k, live, S, M->d_dprecon, M->d_dprecon32);
+    if (st != SG_OK) {
+      // the reference stops the program on a PCG failure (error_stop, src/slope.F90:294)
+      for (int t = 0; t < k; ++t)
+        if (live[t]) { res[t].errcode = st; res[t].nl_iter = nl_iter; live[t] = 0; }
+      status = st;
+      break;
+    }
+    for (int t = 0; t < k; ++t)
+      if (live[t]) { res[t].cg_tot += S.iters[t]; res[t].refine_steps += S.refine; }
+    if (ctl->allelastic) {
+      for (int t = 0; t < k; ++t) {
+        if (!live[t]) continue;
+        launch_elastic_stress(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, W.x + 0, W.mf + (size_t)t * h.nmatblk, 0,
+                              W.stress + nst * t, s);
+        res[t].nl_iter = nl_iter; res[t].converged = 0; res[t].failed = (nl_iter == ctl->nl_maxiter);
+        live[t] = 0;
+      }
+      break;
+    }
+    // uerr = max|x-oldx| / max|x|; oldx = x (src/slope.F90:307-309)
+    launch_nl_check(n1, KR, k, W.x, W.oldx, W.b64.part, s);
+    reduce_read(c, W.b64.part, NPART, KR, 2, 3, W.red, red);
+    int mask[16] = {0};
+    std::vector<int> fin(k, 0), conv(k, 0);
+    for (int t = 0; t < k; ++t) {
+      if (!live[t]) continue;
+      double uerr = red[2 * t] / red[2 * t + 1];
+      res[t].uerr = uerr;
+      conv[t] = uerr <= ctl->nl_tol;
+      fin[t] = conv[t] || nl_iter == ctl->nl_maxiter;
+      mask[t] = 1;
+      int ev = c->prof_begin();
+      launch_stress_update(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, W.x, KR, t, W.mf + (size_t)t * h.nmatblk,
+                           dt[t], conv[t], fin[t], W.evpt + nst * t, W.stress + nst * t, W.Yb, KR, t,
+                           M->d_fpart + NPART * (t & 1), s);
+      c->prof_end(ev, 4);
+      reduce_read(c, M->d_fpart + NPART * (t & 1), NPART, 1, 1, 1, W.red, red + 32);
+      res[t].fmax = red[32];
+    }
+    // bodyload(egdof) += bload for the trials that continue
+    int gmask[16] = {0};
+    bool anyg = false;
+    for (int t = 0; t < k; ++t) { gmask[t] = mask[t] && !fin[t]; anyg = anyg || gmask[t]; }
+    if (anyg) {
+      cudaMemcpyAsync(W.colmask, gmask, sizeof(int) * 16, cudaMemcpyHostToDevice, s);
+      launch_gather_plain<double>(M->T, KR, W.Yb, W.bodyload, 1, W.colmask, s);
+    }
+    for (int t = 0; t < k; ++t) {
+      if (!live[t] || !fin[t]) continue;
+      res[t].nl_iter = nl_iter;
+      res[t].converged = conv[t];
+      res[t].failed = (nl_iter == ctl->nl_maxiter);
+      live[t] = 0;
+    }
+  }
+  // summary maxima (src/slope.F90:400-415)
+  for (int t = 0; t < k; ++t) {
+    launch_disp_max(h.nnode, M->d_gdof, W.x, KR, t, W.b64.part, s);
+    reduce_read(c, W.b64.part, NPART, 1, 2, 3, W.red, red);
+    res[t].uxmax = red[0];
+    res[t].umax = red[1];
+  }
+  if (x_out) {
+    std::vector<double> hx(nv);
+    cudaMemcpy(hx.data(), W.x, sizeof(double) * nv, cudaMemcpyDeviceToHost);
+    for (int t = 0; t < k; ++t)
+      for (int i = 0; i < n1; ++i) x_out[(size_t)t * n1 + i] = hx[(size_t)i * KR + t];
+  }
+  if (restiff) {
+    model_stiffness(M, nullptr, ne, M->d_nu, M->T, M->d_ge, n1, false);
+    c->release(d_nuf);
+  }
+  if (!c->check(cudaStreamSynchronize(s), "trials")) status = SG_ERR_CUDA;
+  double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  for (int t = 0; t < k; ++t) res[t].seconds = secs;
+  return status;
+}
+
+extern "C" {
+
+int sg_srf_trials(sg_model* M, const sg_control* ctl, int k, const double* srf, sg_trial_result* results,
+                  double* x_out) {
+  if (!M) return SG_ERR_BADARG;
+  return run_trials(M, ctl, k, srf, results, x_out);
+}
+
+int sg_last_stress(sg_model* M, int trial, double* stress_elmt) {
+  if (!M || !stress_elmt || trial < 0 || trial >= M->W.KR) return SG_ERR_BADARG;
+  size_t nst = (size_t)M->H.nelmt * NGLL * NST;
+  cudaMemcpy(stress_elmt, M->W.stress + nst * trial, sizeof(double) * nst, cudaMemcpyDeviceToHost);
+  return SG_OK;
+}
+
+int sg_srf_sweep(sg_model* M, const sg_control* ctl, int nsrf, const double* srf, sg_trial_result* results,
+                 int* ndone) {
+  if (!M || nsrf < 1) return SG_ERR_BADARG;
+  int n = 0, st = SG_OK;
+  for (int i = 0; i < nsrf; ++i) {
+    st = run_trials(M, ctl, 1, srf + i, results + i, nullptr);
+    ++n;
+    if (st != SG_OK || results[i].failed) break;
+  }
+  if (ndone) *ndone = n;
+  return st;
+}
+
+// Critical SRF on a grid by k-section: each round probes k grid points spread
+// evenly inside the current bracket (a, b) as one batched trial set, then
+// keeps the sub-interval between the last stable and the first failed probe.
+int sg_fos(sg_model* M, const sg_control* ctl, double lo, double hi, double step, int k, double* fos, int* ntrials,
+           int* nrounds) {
+  if (!M || !ctl || step <= 0 || hi <= lo || k < 1 || k > 16 || !fos) return SG_ERR_BADARG;
+  int Mg = (int)std::lround((hi - lo) / step);
+  int a = 0, b = Mg, nt = 0, nr = 0;
+  while (b - a > 1) {
+    int gap = b - a - 1;
+    int kk = std::min(k, gap);
+    std::vector<int> probe(kk);
+    for (int t = 0; t < kk; ++t) probe[t] = a + (int)(((long long)(t + 1) * (b - a)) / (kk + 1));
+    probe.erase(std::unique(probe.begin(), probe.end()), probe.end());
+    kk = (int)probe.size();
+    std::vector<double> srf(kk);
+    for (int t = 0; t < kk; ++t) srf[t] = lo + step * probe[t];
+    std::vector<sg_trial_result> res(kk);
+    int st = run_trials(M, ctl, kk, srf.data(), res.data(), nullptr);
+    nt += kk;
+    ++nr;
+    if (st != SG_OK) return st;
+    int na = a, nb = b;
+    for (int t = 0; t < kk; ++t) {
+      if (res[t].failed) { nb = probe[t]; break; }
+      na = probe[t];
+    }
+    a = na;
+    b = nb;
+  }
+  *fos = lo + step * b;
+  if (ntrials) *ntrials = nt;
+  if (nrounds) *nrounds = nr;
+  return SG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// excavation3d (src/excavation.F90:15-709) with nsrf = 1
+// ---------------------------------------------------------------------------
+extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, double z0, double s0, double k0,
+                             int nexcav, const int* nexcavid, const int* excavid, int ninc, double srf,
+                             double* stage_res, int* nstage) {
+  if (!M || !ctl || nexcav < 1 || !nexcavid || !excavid || ninc < 1 || !stage_res) return SG_ERR_BADARG;
+  sg_ctx* c = M->ctx;
+  HostMesh& h = M->H;
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  const int ne = h.nelmt, nm = h.nmatblk;
+  const size_t nst = (size_t)ne * NGLL * NST;
+  // persistent stress state
+  double* stress = c->alloc<double>(nst);
+  double* evpt = c->alloc<double>(nst);
+  if (!stress || !evpt) { c->release(stress); c->release(evpt); return SG_ERR_OOM; }
+  cudaMemsetAsync(stress, 0, sizeof(double) * nst, s);
+  std::vector<double> cohf, nuf, phif, psif;
+  std::vector<MatF> mf0;
+  make_matf(h, h.ym, h.nu, h.phi, h.coh, h.psi, mf0);
+  MatF* d_mf = c->alloc<MatF>(nm);
+  cudaMemcpyAsync(d_mf, mf0.data(), sizeof(MatF) * nm, cudaMemcpyHostToDevice, s);
+  int status = SG_OK;
+  if (s0_type == 1) {
+    launch_overburden(M->d_coord, M->d_gnum, M->d_matid, M->d_gam, ne, z0, s0, k0, stress, s);
+  } else if (s0_type == 0) {
+    // gravity solve with the full mesh (src/excavation.F90:182-238)
+    sg_control c0 = *ctl;
+    int KR = 1, n1 = h.neq + 1;
+    if (!model_work(M, KR, n1, ne)) { status = SG_ERR_OOM; goto done; }
+    {
+      cudaMemsetAsync(M->W.x, 0, sizeof(double) * n1, s);
+      cudaMemcpyAsync(M->W.load, M->d_extload, sizeof(double) * n1, cudaMemcpyDeviceToDevice, s);
+      Op op64, op32;
+      op64.K = M->d_K64; op64.ge = M->d_ge; op64.nelmt = ne; op64.T = &M->T;
+      op32 = op64; op32.K = M->d_K32;
+      SolveStats S;
+      std::vector<int> act(1, 1);
+      status = linear_solve(M, &c0, op64, op32, 1, act, S, M->d_dprecon, M->d_dprecon32);
+      if (status != SG_OK) goto done;
+      launch_elastic_stress(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, M->W.x, d_mf, 0, stress, s);
+    }
+  } else {
+    status = SG_ERR_BADARG;
+    goto done;
+  }
+  {
+    std::vector<char> ismat(nm, 1);
+    std::vector<int> gdof = h.gdof;
+    std::vector<double> nodalu((size_t)3 * h.nnode, 0.0);
+    std::vector<int> ge_all((size_t)ne * NEDOF);
+    int stages = 0;
+    for (int is = 0; is < nexcav; ++is) {
+      // id0 = (i_excav-1)*nexcavid(i_excav)+1 (src/excavation.F90:339), kept as in the reference
+      int id0 = is * nexcavid[is];
+      std::vector<char> off(nm, 0);
+      for (int i = id0; i < id0 + nexcavid[is]; ++i) {
+        if (excavid[i] < 1 || excavid[i] > nm) { status = SG_ERR_BADARG; goto done; }
+        ismat[excavid[i] - 1] = 0;
+        off[excavid[i] - 1] = 1;
+      }
+      std::vector<int> eint, evoid;
+      for (int e = 0; e < ne; ++e) {
+        int im = h.mat_id[e] - 1;
+        if (off[im]) evoid.push_back(e);
+        else if (ismat[im]) eint.push_back(e);
+      }
+      if (eint.empty()) break;
+      std::vector<char> isnode(h.nnode, 0);
+      for (int e : eint)
+        for (int a = 0; a < NGLL; ++a) isnode[h.g_num[(size_t)e * NGLL + a]] = 1;
+      // modify_gdof (src/excavation_library.f90:90-111)
+      for (int j = 0; j < h.nnode; ++j)
+        if (!isnode[j]) gdof[3 * j] = gdof[3 * j + 1] = gdof[3 * j + 2] = 0;
+      int neq = 0;
+      for (int j = 0; j < h.nnode; ++j)
+        for (int d = 0; d < 3; ++d)
+          if (gdof[3 * j + d]) gdof[3 * j + d] = ++neq;
+      const int n1 = neq + 1, nint = (int)eint.size(), nvoid = (int)evoid.size();
+      for (int e = 0; e < ne; ++e)
+        for (int a = 0; a < NGLL; ++a)
+          for (int d = 0; d < 3; ++d) ge_all[(size_t)e * NEDOF + 3 * a + d] = gdof[3 * h.g_num[(size_t)e * NGLL + a] + d];
+      std::vector<int> ge_int((size_t)nint * NEDOF), ge_void((size_t)std::max(nvoid, 1) * NEDOF, 0);
+      for (int i = 0; i < nint; ++i)
+        std::memcpy(&ge_int[(size_t)i * NEDOF], &ge_all[(size_t)eint[i] * NEDOF], sizeof(int) * NEDOF);
+      for (int i = 0; i < nvoid; ++i)
+        std::memcpy(&ge_void[(size_t)i * NEDOF], &ge_all[(size_t)evoid[i] * NEDOF], sizeof(int) * NEDOF);
+      GatherTopo Ti, Tv;
+      build_groups_from_gdof(ge_int.data(), nint, neq, Ti);
+      build_groups_from_gdof(ge_void.data(), nvoid, neq, Tv);
+      int* d_eint = c->alloc<int>(nint);
+      int* d_evoid = c->alloc<int>(std::max(nvoid, 1));
+      int* d_geint = c->alloc<int>(ge_int.size());
+      int* d_geall = c->alloc<int>(ge_all.size());
+      int* d_gdofn = c->alloc<int>(gdof.size());
+      bool ok = d_eint && d_evoid && d_geint && d_geall && d_gdofn && upload_topo(c, Ti) && upload_topo(c, Tv) &&
+                model_work(M, 1, n1, nint);
+      if (!ok) {
+        status = SG_ERR_OOM;
+      } else {
+        cudaMemcpyAsync(d_eint, eint.data(), sizeof(int) * nint, cudaMemcpyHostToDevice, s);
+        if (nvoid) cudaMemcpyAsync(d_evoid, evoid.data(), sizeof(int) * nvoid, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_geint, ge_int.data(), sizeof(int) * ge_int.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_geall, ge_all.data(), sizeof(int) * ge_all.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_gdofn, gdof.data(), sizeof(int) * gdof.size(), cudaMemcpyHostToDevice, s);
+        TrialWork& W = M->W;
+        // K9 release load of the removed elements -> extload (distribute2ghosts, src/serial_library.f90:110-130)
+        double* Ye = M->d_Yscratch;
+        cudaMemsetAsync(M->d_extload, 0, sizeof(double) * n1, s);
+        if (nvoid) {
+          launch_release_load(M->d_geo, d_evoid, nvoid, M->d_matid, M->d_gam, stress, Ye, s);
+          launch_gather_plain<double>(Tv, 1, Ye, M->d_extload, 0, nullptr, s);
+        }
+        launch_div((size_t)n1, M->d_extload, (double)ninc, s);
+        // strength reduction, dt over the intact materials, stiffness of intact elements
+        strength_reduction(h, srf, ctl->phinu != 0, cohf, nuf, phif, psif);
+        double dt = dt_viscoplas(nuf, phif, h.ym, &ismat);
+        std::vector<MatF> mf;
+        make_matf(h, h.ym, nuf, phif, cohf, psif, mf);
+        cudaMemcpyAsync(W.mf, mf.data(), sizeof(MatF) * nm, cudaMemcpyHostToDevice, s);
+        double* d_nuf = c->alloc<double>(nm);
+        cudaMemcpyAsync(d_nuf, nuf.data(), sizeof(double) * nm, cudaMemcpyHostToDevice, s);
+        model_stiffness(M, d_eint, nint, d_nuf, Ti, d_geint, n1, false);
+        c->release(d_nuf);
+        Op op64, op32;
+        op64.K = M->d_K64; op64.ge = d_geint; op64.nelmt = nint; op64.T = &Ti;
+        op32 = op64; op32.K = M->d_K32;
+        int cg_tot = 0, nl_tot = 0, nl_iter = 0;
+        double fmax = 0.0, red[64];
+        for (int inc = 0; inc < ninc && status == SG_OK; ++inc) {
+          cudaMemsetAsync(W.bodyload, 0, sizeof(double) * n1, s);
+          cudaMemsetAsync(evpt, 0, sizeof(double) * nst, s);
+          cudaMemsetAsync(W.x, 0, sizeof(double) * n1, s);
+          cudaMemsetAsync(W.oldx, 0, sizeof(double) * n1, s);
+          for (nl_iter = 1; nl_iter <= ctl->nl_maxiter; ++nl_iter) {
+            launch_load_combine(n1, 1, M->d_extload, W.bodyload, W.load, s);
+            SolveStats S;
+            std::vector<int> act(1, 1);
+            int st = linear_solve(M, ctl, op64, op32, 1, act, S, M->d_dprecon, M->d_dprecon32);
+            if (st != SG_OK) { status = st; break; }
+            cg_tot += S.iters[0];
+            launch_nl_check(n1, 1, 1, W.x, W.oldx, W.b64.part, s);
+            reduce_read(c, W.b64.part, NPART, 1, 2, 3, W.red, red);
+            double uerr = red[0] / red[1];
+            int conv = uerr <= ctl->nl_tol, fin = conv || nl_iter == ctl->nl_maxiter;
+            launch_stress_update(M->d_geo, d_eint, nint, d_geall, M->d_matid, W.x, 1, 0, W.mf, dt, conv, fin, evpt,
+                                 stress, W.Yb, 1, 0, M->d_fpart, s);
+            reduce_read(c, M->d_fpart, NPART, 1, 1, 1, W.red, red);
+            fmax = red[0];
+            if (!fin) launch_gather_plain<double>(Ti, 1, W.Yb, W.bodyload, 1, nullptr, s);
+            if (fin) break;
+          }
+          if (nl_iter > ctl->nl_maxiter) nl_iter = ctl->nl_maxiter;
+          nl_tot += nl_iter;
+          // nodalu += x (src/excavation.F90:631-637)
+          std::vector<double> hx(n1);
+          cudaMemcpy(hx.data(), W.x, sizeof(double) * n1, cudaMemcpyDeviceToHost);
+          for (int j = 0; j < h.nnode; ++j)
+            for (int d = 0; d < 3; ++d)
+              if (gdof[3 * j + d]) nodalu[3 * j + d] += hx[gdof[3 * j + d]];
+        }
+        double uxmax = 0, umax = 0;
+        for (int j = 0; j < h.nnode; ++j) {
+          if (!isnode[j]) continue;
+          const double* u = &nodalu[3 * j];
+          for (int d = 0; d < 3; ++d) uxmax = std::max(uxmax, std::fabs(u[d]));
+          umax = std::max(umax, std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+        }
+        double* r = stage_res + 8 * is;
+        r[0] = is + 1; r[1] = cg_tot; r[2] = nl_tot; r[3] = uxmax; r[4] = umax; r[5] = fmax;
+        r[6] = (nl_iter == ctl->nl_maxiter); r[7] = status;
+        ++stages;
+        if (nl_iter == ctl->nl_maxiter) { /* the reference stops the stage loop */ }
+      }
+      free_topo(c, Ti);
+      free_topo(c, Tv);
+      for (void* p : {(void*)d_eint, (void*)d_evoid, (void*)d_geint, (void*)d_geall, (void*)d_gdofn}) c->release(p);
+      if (status != SG_OK || stage_res[8 * is + 6] != 0) break;
+    }
+    if (nstage) *nstage = stages;
+    // restore the full-mesh stiffness for later trials on this model
+    model_stiffness(M, nullptr, ne, M->d_nu, M->T, M->d_ge, h.neq + 1, true);
+  }
+done:
+  c->release(stress);
+  c->release(evpt);
+  c->release(d_mf);
+  if (!c->check(cudaStreamSynchronize(s), "excavation") && status == SG_OK) status = SG_ERR_CUDA;
+  return status;
+}

@@ -1,0 +1,1192 @@
+// sg_kernels.cu -- sm_103a kernels of the solve path.
+//
+//   apply     element-by-element operator Y_e = K_e p_e (src/solver.f90:53-58):
+//             dense FP64 81x81 (the drop-in's caller-provided matrices) and the
+//             sparse symmetric GLL layout (FP64 or FP32, 1..16 right-hand sides)
+//   gather    deterministic scatter-add: every free dof sums its element
+//             contributions in increasing element order, fused with the PCG
+//             direction update and the p.kp dot (src/solver.f90:53-62)
+//   update    fused u, r, z update, max-norms, r.z and the step stop test
+//             (src/solver.f90:63-73) with last-block finalisation
+//   geometry  Jacobian inverse and determinant per GLL point (src/preprocess.f90:112-118)
+//   stiffness K6, element matrices, diagonal and gravity load (src/preprocess.f90:74-148)
+//   stress    K5, strain, Mohr-Coulomb yield, viscoplastic flow and body load
+//             (src/slope.F90:311-383, src/excavation.F90:546-616)
+//
+// All reductions use a fixed grid (NPART blocks) and fixed-order trees, so a
+// run is bitwise reproducible on the same device type.
+#include <cstdio>
+#include <type_traits>
+
+#include "sg_kernels.cuh"
+
+namespace sg {
+
+// D[p][m] = derivative of the m-th 1D Lagrange polynomial on the GLL points
+// {-1, 0, 1} evaluated at point p (lagrange1dGLL, src/gll_library.f90:257-299);
+// all entries are exact in binary floating point.
+__constant__ double c_D[3][3];
+__constant__ double c_w[NGLL];             // gll_weights (src/gll_library.f90:46-60)
+__constant__ double c_dshape[3][8][NGLL];  // dshape_hex8 (src/shape_library.f90:104-216)
+__constant__ int c_gnode[8];               // hex8_gnode (src/element.f90:21-45)
+
+void upload_constants() {
+  static bool done = false;
+  if (done) return;
+  const double D[3][3] = {{-1.5, 2.0, -0.5}, {-0.5, 0.0, 0.5}, {0.5, -2.0, 1.5}};
+  const double xi[3] = {-1.0, 0.0, 1.0}, w1[3] = {1.0 / 3.0, 4.0 / 3.0, 1.0 / 3.0};
+  double w[NGLL], ds[3][8][NGLL];
+  const double e8 = 0.125;
+  int n = 0;
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < 3; ++j)
+      for (int i = 0; i < 3; ++i, ++n) {
+        w[n] = w1[i] * w1[j] * w1[k];
+        double xp = 1 + xi[i], xm = 1 - xi[i], ep = 1 + xi[j], em = 1 - xi[j], zp = 1 + xi[k], zm = 1 - xi[k];
+        ds[0][0][n] = -e8 * em * zm; ds[0][1][n] = e8 * em * zm; ds[0][2][n] = e8 * ep * zm; ds[0][3][n] = -e8 * ep * zm;
+        ds[0][4][n] = -e8 * em * zp; ds[0][5][n] = e8 * em * zp; ds[0][6][n] = e8 * ep * zp; ds[0][7][n] = -e8 * ep * zp;
+        ds[1][0][n] = -e8 * xm * zm; ds[1][1][n] = -e8 * xp * zm; ds[1][2][n] = e8 * xp * zm; ds[1][3][n] = e8 * xm * zm;
+        ds[1][4][n] = -e8 * xm * zp; ds[1][5][n] = -e8 * xp * zp; ds[1][6][n] = e8 * xp * zp; ds[1][7][n] = e8 * xm * zp;
+        ds[2][0][n] = -e8 * xm * em; ds[2][1][n] = -e8 * xp * em; ds[2][2][n] = -e8 * xp * ep; ds[2][3][n] = -e8 * xm * ep;
+        ds[2][4][n] = e8 * xm * em; ds[2][5][n] = e8 * xp * em; ds[2][6][n] = e8 * xp * ep; ds[2][7][n] = e8 * xm * ep;
+      }
+  const int gn[8] = {0, 2, 8, 6, 18, 20, 26, 24};
+  cudaMemcpyToSymbol(c_D, D, sizeof(D));
+  cudaMemcpyToSymbol(c_w, w, sizeof(w));
+  cudaMemcpyToSymbol(c_dshape, ds, sizeof(ds));
+  cudaMemcpyToSymbol(c_gnode, gn, sizeof(gn));
+  done = true;
+}
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename V>
+__device__ __forceinline__ V fmav(V a, V b, V c);
+template <>
+__device__ __forceinline__ double fmav<double>(double a, double b, double c) { return fma(a, b, c); }
+template <>
+__device__ __forceinline__ float fmav<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// p_new = z + beta*p, rounded the same way wherever it is formed.
+template <typename V>
+__device__ __forceinline__ V pdir(double beta, V p, V z) {
+  return (V)fma(beta, (double)p, (double)z);
+}
+
+// Per-column block reduction of `val` (threads whose index = j mod KR hold
+// column j).  Result for column j lands in out[j] on thread 0..KR-1 of warp 0.
+// op 0 = sum, 1 = max.  Fixed tree order.
+template <int KR>
+__device__ __forceinline__ double warp_col_reduce(double v, int op) {
+#pragma unroll
+  for (int o = 16; o >= KR; o >>= 1) {
+    double w = __shfl_xor_sync(FULL, v, o);
+    v = op ? fmax(v, w) : v + w;
+  }
+  return v;
+}
+
+// last-block election: returns true in the block that finished last.
+__device__ __forceinline__ bool last_block(unsigned* counter) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = atomicAdd(counter, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) __threadfence();
+  return am_last;
+}
+
+// ---------------------------------------------------------------------------
+// Geometry cache: Jacobian of the hex8 map at each GLL point, its determinant
+// and its inverse (determinant/invert, src/math_library.f90:66-138).
+// geo[(e*27+i)*10 + 3*d + a] = Jinv(d,a); geo[..+9] = detJ.
+// ---------------------------------------------------------------------------
+__global__ void k_geometry(const double* __restrict__ g_coord, const int* __restrict__ g_num, int nelmt,
+                           double* __restrict__ geo) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nelmt * NGLL) return;
+  int e = t / NGLL, i = t - e * NGLL;
+  double coord[8][3];
+#pragma unroll
+  for (int g = 0; g < 8; ++g) {
+    int nd = g_num[(size_t)e * NGLL + c_gnode[g]];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) coord[g][b] = g_coord[(size_t)3 * nd + b];
+  }
+  double x[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      double s = 0.0;
+#pragma unroll
+      for (int g = 0; g < 8; ++g) s = __dadd_rn(s, __dmul_rn(c_dshape[a][g][i], coord[g][b]));
+      x[a][b] = s;
+    }
+  double det = x[0][0] * (x[1][1] * x[2][2] - x[2][1] * x[1][2]);
+  det = det - x[0][1] * (x[1][0] * x[2][2] - x[2][0] * x[1][2]);
+  det = det + x[0][2] * (x[1][0] * x[2][1] - x[2][0] * x[1][1]);
+  double j11 = x[1][1] * x[2][2] - x[2][1] * x[1][2];
+  double j21 = -x[1][0] * x[2][2] + x[2][0] * x[1][2];
+  double j31 = x[1][0] * x[2][1] - x[2][0] * x[1][1];
+  double j12 = -x[0][1] * x[2][2] + x[2][1] * x[0][2];
+  double j22 = x[0][0] * x[2][2] - x[2][0] * x[0][2];
+  double j32 = -x[0][0] * x[2][1] + x[2][0] * x[0][1];
+  double j13 = x[0][1] * x[1][2] - x[1][1] * x[0][2];
+  double j23 = -x[0][0] * x[1][2] + x[1][0] * x[0][2];
+  double j33 = x[0][0] * x[1][1] - x[1][0] * x[0][1];
+  double* o = geo + (size_t)t * GEO_STRIDE;
+  o[0] = j11 / det; o[1] = j12 / det; o[2] = j13 / det;
+  o[3] = j21 / det; o[4] = j22 / det; o[5] = j23 / det;
+  o[6] = j31 / det; o[7] = j32 / det; o[8] = j33 / det;
+  o[9] = det;
+}
+
+void launch_geometry(const double* g_coord, const int* g_num, int nelmt, double* geo, cudaStream_t s) {
+  int n = nelmt * NGLL;
+  k_geometry<<<(n + 127) / 128, 128, 0, s>>>(g_coord, g_num, nelmt, geo);
+}
+
+// deriv(:,n) at GLL point i: sum_a Jinv(:,a) dlagrange(a,i,n).  dlagrange is
+// non-zero only for nodes on the three lattice lines through i, where it is
+// D[i_a][n_a]; the zero terms of the reference sum are skipped (they add +0).
+__device__ __forceinline__ bool on_line(int i, int n) {
+  int dx = (i % 3) != (n % 3), dy = ((i / 3) % 3) != ((n / 3) % 3), dz = (i / 9) != (n / 9);
+  return dx + dy + dz <= 1;
+}
+__device__ __forceinline__ void point_grad(const double* __restrict__ Ji, int i, int n, double g[3]) {
+  int ic[3] = {i % 3, (i / 3) % 3, i / 9}, nc[3] = {n % 3, (n / 3) % 3, n / 9};
+  double dl[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    bool same_other = true;
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      if (b != a && ic[b] != nc[b]) same_other = false;
+    dl[a] = same_other ? c_D[ic[a]][nc[a]] : 0.0;
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double s = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) s = s + Ji[3 * d + a] * dl[a];
+    g[d] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K6: element stiffness in the sparse symmetric layout.
+// K(3n+c,3m+d) = sum_i w_i detJ_i [B_i^T C B_i](3n+c,3m+d) with the isotropic
+// C of compute_cmat: for c = d, C11 g_n[c] g_m[c] + C44 sum_{e!=c} g_n[e] g_m[e];
+// for c != d, C12 g_n[c] g_m[d] + C44 g_n[d] g_m[c]  (g = deriv columns).
+// One block per element; threads loop over the 2430 stored entries.
+// ---------------------------------------------------------------------------
+constexpr int STIFF_THREADS = 256;
+
+__global__ void __launch_bounds__(STIFF_THREADS) k_stiffness(
+    const double* __restrict__ geo, const int* __restrict__ mat_id, const int* __restrict__ elist, int nel,
+    const double* __restrict__ ym, const double* __restrict__ nu, const double* __restrict__ gam,
+    double* __restrict__ Ks64, float* __restrict__ Ks32, double* __restrict__ Ydiag, double* __restrict__ Ygrav,
+    const int* __restrict__ entry) {
+  __shared__ double sg[NGLL][NGLL][3];   // grad of node n at point i (zero off the lines)
+  __shared__ double sgeo[NGLL][GEO_STRIDE];
+  __shared__ double swd[NGLL];
+  const int le = blockIdx.x;
+  if (le >= nel) return;
+  const int e = elist ? elist[le] : le;
+  const int im = mat_id[e] - 1;
+  // compute_cmat (src/elastic.f90:13-42)
+  const double E = ym[im], v = nu[im];
+  const double onepv = 1.0 + v, onemv = 1.0 - v, onem2v = 1.0 - 2.0 * v;
+  const double Ef = E / (onepv * onem2v);
+  const double c11 = onemv * Ef, c12 = v * Ef, c44 = 0.5 * onem2v * Ef;
+  for (int t = threadIdx.x; t < NGLL * GEO_STRIDE; t += blockDim.x)
+    sgeo[t / GEO_STRIDE][t % GEO_STRIDE] = geo[(size_t)e * NGLL * GEO_STRIDE + t];
+  __syncthreads();
+  for (int t = threadIdx.x; t < NGLL; t += blockDim.x) swd[t] = sgeo[t][9] * c_w[t];
+  for (int t = threadIdx.x; t < NGLL * NGLL; t += blockDim.x) {
+    int i = t / NGLL, n = t % NGLL;
+    double g[3] = {0.0, 0.0, 0.0};
+    if (on_line(i, n)) point_grad(sgeo[i], i, n, g);
+    sg[i][n][0] = g[0]; sg[i][n][1] = g[1]; sg[i][n][2] = g[2];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < KS_NNZ; t += blockDim.x) {
+    int pk = entry[t];
+    int row = pk & 255, col = pk >> 8;
+    int n = row / 3, c = row % 3, m = col / 3, d = col % 3;
+    if (n == m && c > d) { int tmp = c; c = d; d = tmp; }  // exact symmetry inside own-node blocks
+    double acc = 0.0;
+    for (int i = 0; i < NGLL; ++i) {
+      if (!on_line(i, n) || !on_line(i, m)) continue;
+      const double* gn = sg[i][n];
+      const double* gm = sg[i][m];
+      double b;
+      if (c == d) {
+        int e1 = (c + 1) % 3, e2 = (c + 2) % 3;
+        b = c11 * gn[c] * gm[c] + c44 * (gn[e1] * gm[e1] + gn[e2] * gm[e2]);
+      } else {
+        b = c12 * gn[c] * gm[d] + c44 * gn[d] * gm[c];
+      }
+      acc = acc + b * swd[i];
+    }
+    size_t o = (size_t)le * KS_STRIDE + t;
+    if (Ks64) Ks64[o] = acc;
+    if (Ks32) Ks32[o] = (float)acc;
+    if (row == col && Ydiag) Ydiag[(size_t)le * NEDOF + row] = acc;
+  }
+  if (Ks64 || Ks32)
+    for (int t = KS_NNZ + threadIdx.x; t < KS_STRIDE; t += blockDim.x) {
+      if (Ks64) Ks64[(size_t)le * KS_STRIDE + t] = 0.0;
+      if (Ks32) Ks32[(size_t)le * KS_STRIDE + t] = 0.0f;
+    }
+  // gravity: extload(egdof) -= eld*gam, eld non-zero on z dofs = detJ*w
+  // (src/preprocess.f90:123-136); stored as the negated contribution.
+  if (Ygrav)
+    for (int t = threadIdx.x; t < NEDOF; t += blockDim.x) {
+      int a = t / 3, d = t % 3;
+      Ygrav[(size_t)le * NEDOF + t] = (d == 2) ? -(swd[a] * gam[im]) : -0.0;
+    }
+}
+
+void launch_stiffness(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
+                      const double* nu, const double* gam, double* Ks64, float* Ks32, double* Ydiag,
+                      double* Ygrav, const int* d_entry, cudaStream_t s) {
+  if (nel <= 0) return;
+  k_stiffness<<<nel, STIFF_THREADS, 0, s>>>(geo, mat_id, elist, nel, ym, nu, gam, Ks64, Ks32, Ydiag, Ygrav,
+                                           d_entry);
+}
+
+// Expand the sparse symmetric layout to the reference's dense column-major
+// 81x81 storage (for export and for checks).
+__global__ void k_expand_dense(const double* __restrict__ Ks, int nel, double* __restrict__ dense,
+                               const int* __restrict__ entry) {
+  int e = blockIdx.x;
+  if (e >= nel) return;
+  double* D = dense + (size_t)e * NEDOF * NEDOF;
+  for (int t = threadIdx.x; t < NEDOF * NEDOF; t += blockDim.x) D[t] = 0.0;
+  __syncthreads();
+  for (int t = threadIdx.x; t < KS_NNZ; t += blockDim.x) {
+    int pk = entry[t], row = pk & 255, col = pk >> 8;
+    double v = Ks[(size_t)e * KS_STRIDE + t];
+    D[(size_t)col * NEDOF + row] = v;
+    D[(size_t)row * NEDOF + col] = v;
+  }
+}
+
+void launch_expand_dense(const double* Ks64, int nel, double* dense, const int* d_entry, cudaStream_t s) {
+  if (nel > 0) k_expand_dense<<<nel, 256, 0, s>>>(Ks64, nel, dense, d_entry);
+}
+
+// ---------------------------------------------------------------------------
+// Element apply.
+// ---------------------------------------------------------------------------
+constexpr int APPLY_WARPS = 4;
+
+// Dense FP64 81x81, one right-hand side (the drop-in).  One warp per element,
+// lane l owns rows l, l+32, l+64; column c of K_e is 81 contiguous doubles,
+// read once with a streaming hint.  combine: p_e = z_e + beta*p_old_e.
+__global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_dense64(
+    const double* __restrict__ K, const int* __restrict__ ge, int nelmt, const double* __restrict__ pold,
+    const double* __restrict__ z, int combine, double* __restrict__ Y, const ColState* __restrict__ cs,
+    const PcgGlobal* __restrict__ G) {
+  if (G && G->all_done) return;
+  const int lane = threadIdx.x & 31;
+  const int w0 = blockIdx.x * APPLY_WARPS + (threadIdx.x >> 5);
+  const double beta = combine ? cs[0].beta : 0.0;
+  for (int e = w0; e < nelmt; e += gridDim.x * APPLY_WARPS) {
+    const int* g = ge + (size_t)e * NEDOF;
+    int g0 = g[lane], g1 = g[lane + 32], g2 = lane < 17 ? g[lane + 64] : 0;
+    double p0 = pold[g0], p1 = pold[g1], p2 = lane < 17 ? pold[g2] : 0.0;
+    if (combine) {
+      p0 = pdir(beta, p0, z[g0]);
+      p1 = pdir(beta, p1, z[g1]);
+      p2 = lane < 17 ? pdir(beta, p2, z[g2]) : 0.0;
+    }
+    const double* k = K + (size_t)e * NEDOF * NEDOF;
+    double y0 = 0.0, y1 = 0.0, y2 = 0.0;
+#pragma unroll
+    for (int c = 0; c < NEDOF; ++c) {
+      double src = c < 32 ? p0 : (c < 64 ? p1 : p2);
+      double pc = __shfl_sync(FULL, src, c & 31);
+      const double* col = k + (size_t)c * NEDOF;
+      y0 = fma(__ldcs(col + lane), pc, y0);
+      y1 = fma(__ldcs(col + lane + 32), pc, y1);
+      if (lane < 17) y2 = fma(__ldcs(col + lane + 64), pc, y2);
+    }
+    double* yo = Y + (size_t)e * NEDOF;
+    yo[lane] = y0;
+    yo[lane + 32] = y1;
+    if (lane < 17) yo[lane + 64] = y2;
+  }
+}
+
+// Sparse symmetric layout, KR right-hand sides (vectors are [dof][KR]).
+// One warp per element: K_e (KS_STRIDE values) and p_e (81*KR) are staged in
+// shared memory with 16-byte streaming loads, then lane n < 27 forms the
+// three rows of node n from its 19 coupled node blocks.  The lane table nbr
+// gives, per (n, s), the coupled node m, the block offset and whether the
+// stored block is (n,m) (row-major access) or (m,n) (transposed access).
+template <typename V, int KR>
+__global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse(
+    const V* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const V* __restrict__ pold,
+    const V* __restrict__ z, int combine, V* __restrict__ Y, const ColState* __restrict__ cs,
+    const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g) {
+  if (G && G->all_done) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  int* nbr = (int*)smem;                                   // 27*19 ints (2064 B incl. pad)
+  V* wbase = (V*)(smem + 2064);
+  constexpr int WSTRIDE = KS_STRIDE + ((NEDOF * KR + 3) & ~3);  // keeps every warp region 16-byte aligned
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  V* ks = wbase + warp * WSTRIDE;
+  V* ps = ks + KS_STRIDE;
+  for (int t = threadIdx.x; t < NGLL * KS_NBR; t += blockDim.x) nbr[t] = nbr_g[t];
+  double beta[KR];
+#pragma unroll
+  for (int j = 0; j < KR; ++j) beta[j] = combine ? cs[j].beta : 0.0;
+  __syncthreads();
+  constexpr int NV = KS_STRIDE * (int)sizeof(V) / 16;
+  for (int e = blockIdx.x * APPLY_WARPS + warp; e < nelmt; e += gridDim.x * APPLY_WARPS) {
+    const float4* src = reinterpret_cast<const float4*>(Ks + (size_t)e * KS_STRIDE);
+    float4* dst = reinterpret_cast<float4*>(ks);
+#pragma unroll 4
+    for (int q = lane; q < NV; q += 32) dst[q] = __ldcs(src + q);
+    if (lane < NGLL) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        int g = ge[(size_t)e * NEDOF + 3 * lane + d];
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          V pv = pold[(size_t)g * KR + j];
+          if (combine) pv = pdir(beta[j], pv, z[(size_t)g * KR + j]);
+          ps[(3 * lane + d) * KR + j] = pv;
+        }
+      }
+    }
+    __syncwarp();
+    if (lane < NGLL) {
+      V acc[3][KR];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int j = 0; j < KR; ++j) acc[c][j] = (V)0;
+      const int* tb = nbr + lane * KS_NBR;
+#pragma unroll 1
+      for (int s = 0; s < KS_NBR; ++s) {
+        int pk = tb[s];
+        int m = pk & 31, kind = (pk >> 5) & 3, off = pk >> 8;
+        int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
+        const V* kb = ks + off;
+        const V* pm = ps + 3 * m * KR;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            V kv = kb[c * sc + d * sd];
+#pragma unroll
+            for (int j = 0; j < KR; ++j) acc[c][j] = fmav<V>(kv, pm[d * KR + j], acc[c][j]);
+          }
+        }
+      }
+      V* yo = Y + ((size_t)e * NEDOF + 3 * lane) * KR;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int j = 0; j < KR; ++j) yo[c * KR + j] = acc[c][j];
+    }
+    __syncwarp();
+  }
+}
+
+template <typename V, int KR>
+static size_t apply_sparse_smem() {
+  return 2064 + (size_t)APPLY_WARPS * (KS_STRIDE + ((NEDOF * KR + 3) & ~3)) * sizeof(V);
+}
+
+template <typename V, int KR>
+void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_old, const V* z, int combine, V* Y,
+               const ColState* cs, const PcgGlobal* G, const int* d_nbr, cudaStream_t s) {
+  if (nelmt <= 0) return;
+  int blocks = (nelmt + APPLY_WARPS - 1) / APPLY_WARPS;
+  if (dense) {
+    if constexpr (std::is_same<V, double>::value && KR == 1)
+      k_apply_dense64<<<blocks, APPLY_WARPS * 32, 0, s>>>((const double*)K, ge, nelmt, p_old, z, combine, Y, cs, G);
+    return;
+  }
+  size_t sm = apply_sparse_smem<V, KR>();
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_apply_sparse<V, KR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  k_apply_sparse<V, KR><<<blocks, APPLY_WARPS * 32, sm, s>>>((const V*)K, ge, nelmt, p_old, z, combine, Y, cs, G,
+                                                               d_nbr);
+}
+
+// ---------------------------------------------------------------------------
+// Gather: kp(dof) = sum over the node's element slots, in element order, of Y.
+// mode 0: plain (kp only); mode 1: PCG iteration -- also p = z + beta*p for
+// the node's dofs and the p.kp partial; the last block forms alpha = rz/p.kp.
+// ---------------------------------------------------------------------------
+template <typename V, int KR>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
+    const int* __restrict__ ptr, const int* __restrict__ ent, const int* __restrict__ dof, int ng,
+    const V* __restrict__ Y, V* __restrict__ kp, V* __restrict__ p, const V* __restrict__ z, int mode,
+    ColState* __restrict__ cs, PcgGlobal* __restrict__ G, double* __restrict__ part) {
+  if (G->all_done) return;
+  double dp[KR];
+  bool live[KR];
+  double beta[KR];
+#pragma unroll
+  for (int j = 0; j < KR; ++j) {
+    dp[j] = 0.0;
+    live[j] = cs[j].active && !cs[j].done;
+    beta[j] = cs[j].beta;
+  }
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    V acc[3][KR];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int j = 0; j < KR; ++j) acc[d][j] = (V)0;
+    const int s1 = ptr[g + 1];
+    for (int s = ptr[g]; s < s1; ++s) {
+      const V* y = Y + (size_t)ent[s] * 3 * KR;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int j = 0; j < KR; ++j) acc[d][j] = acc[d][j] + y[d * KR + j];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      int gd = dof[3 * g + d];
+      if (!gd) continue;
+#pragma unroll
+      for (int j = 0; j < KR; ++j) {
+        size_t o = (size_t)gd * KR + j;
+        if (mode == 0) {
+          kp[o] = acc[d][j];
+        } else if (live[j]) {
+          V pn = pdir(beta[j], p[o], z[o]);
+          p[o] = pn;
+          kp[o] = acc[d][j];
+          dp[j] += (double)pn * (double)acc[d][j];
+        }
+      }
+    }
+  }
+  if (mode == 0) return;
+  __shared__ double sred[RED_THREADS / 32][KR];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < KR; ++j) {
+    double v = dp[j];
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0) sred[warp][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < KR) {
+    double v = 0.0;
+    for (int w = 0; w < RED_THREADS / 32; ++w) v += sred[w][threadIdx.x];
+    part[(size_t)blockIdx.x * KR + threadIdx.x] = v;
+  }
+  if (last_block(&G->cntB)) {
+    if (threadIdx.x < KR) {
+      int j = threadIdx.x;
+      double s = 0.0;
+      for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(part + (size_t)b * KR + j);
+      if (cs[j].active && !cs[j].done) cs[j].alpha = cs[j].rz / s;
+    }
+    if (threadIdx.x == 0) G->cntB = 0;
+  }
+}
+
+template <typename V, int KR>
+void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mode, ColState* cs, PcgGlobal* G,
+                double* part, cudaStream_t s) {
+  k_pcg_gather<V, KR><<<NPART, RED_THREADS, 0, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, Y, kp, p, z, mode, cs,
+                                                     G, part);
+}
+
+// Plain gather without PCG state: out = (accumulate ? out : 0) + sum Y.
+template <typename V>
+__global__ void k_gather_plain(const int* __restrict__ ptr, const int* __restrict__ ent, const int* __restrict__ dof,
+                               int ng, int KR, const V* __restrict__ Y, V* __restrict__ out, int accumulate,
+                               const int* __restrict__ colmask) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ng * KR) return;
+  int g = t / KR, j = t - g * KR;
+  if (colmask && !colmask[j]) return;
+  V acc[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int gd = dof[3 * g + d];
+    acc[d] = (accumulate && gd) ? out[(size_t)gd * KR + j] : (V)0;
+  }
+  for (int s = ptr[g]; s < ptr[g + 1]; ++s) {
+    const V* y = Y + (size_t)ent[s] * 3 * KR;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) acc[d] = acc[d] + y[d * KR + j];
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int gd = dof[3 * g + d];
+    if (gd) out[(size_t)gd * KR + j] = acc[d];
+  }
+}
+
+template <typename V>
+void launch_gather_plain(const GatherTopo& T, int KR, const V* Y, V* out, int accumulate, const int* colmask,
+                         cudaStream_t s) {
+  int n = T.ngroups * KR;
+  if (n > 0) k_gather_plain<V><<<(n + 255) / 256, 256, 0, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, KR, Y, out,
+                                                               accumulate, colmask);
+}
+
+// ---------------------------------------------------------------------------
+// PCG update (src/solver.f90:61-73).  init = 1: r = f - kp, z = D r, rz and
+// |r|^2, beta = 0.  init = 0: u += alpha p, r -= alpha kp, z = D r and the
+// partials max|p|, max|u|, r.z, |r|^2; the last block applies the stop test
+// |alpha|*max|p|/max|u| <= tol (mode 0) or |r| <= tol*|r0| (mode 1), then
+// beta = r.z_new / r.z.
+// ---------------------------------------------------------------------------
+template <typename V, int KR>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
+    int n1, V* __restrict__ u, V* __restrict__ r, V* __restrict__ z, const V* __restrict__ p,
+    const V* __restrict__ kp, const V* __restrict__ f, const V* __restrict__ dprecon, int init,
+    ColState* __restrict__ cs, PcgGlobal* __restrict__ G, double* __restrict__ part) {
+  if (G->all_done) return;
+  const int j = threadIdx.x & (KR - 1);
+  const bool live = cs[j].active && (init || !cs[j].done);
+  const double alpha = init ? 0.0 : cs[j].alpha;
+  double mp = 0.0, mu = 0.0, rz = 0.0, rr = 0.0;
+  if (live) {
+    const size_t n = (size_t)n1 * KR;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const size_t row = i / KR;
+      V ri;
+      if (init) {
+        ri = f[i] - kp[i];
+      } else {
+        V pi = p[i];
+        V ui = (V)((double)u[i] + alpha * (double)pi);
+        u[i] = ui;
+        mp = fmax(mp, fabs((double)pi));
+        mu = fmax(mu, fabs((double)ui));
+        ri = (V)((double)r[i] - alpha * (double)kp[i]);
+      }
+      V zi = dprecon[row] * ri;
+      r[i] = ri;
+      z[i] = zi;
+      rz += (double)ri * (double)zi;
+      rr += (double)ri * (double)ri;
+    }
+  }
+  __shared__ double sred[RED_THREADS / 32][KR][4];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  mp = warp_col_reduce<KR>(mp, 1);
+  mu = warp_col_reduce<KR>(mu, 1);
+  rz = warp_col_reduce<KR>(rz, 0);
+  rr = warp_col_reduce<KR>(rr, 0);
+  if (lane < KR) {
+    sred[warp][lane][0] = mp; sred[warp][lane][1] = mu; sred[warp][lane][2] = rz; sred[warp][lane][3] = rr;
+  }
+  __syncthreads();
+  if (threadIdx.x < KR) {
+    double a = 0.0, b = 0.0, c = 0.0, d = 0.0;
+    for (int w = 0; w < RED_THREADS / 32; ++w) {
+      a = fmax(a, sred[w][threadIdx.x][0]); b = fmax(b, sred[w][threadIdx.x][1]);
+      c += sred[w][threadIdx.x][2]; d += sred[w][threadIdx.x][3];
+    }
+    double* o = part + ((size_t)blockIdx.x * KR + threadIdx.x) * 4;
+    o[0] = a; o[1] = b; o[2] = c; o[3] = d;
+  }
+  if (!last_block(&G->cntC)) return;
+  __shared__ int s_alldone;
+  if (threadIdx.x == 0) s_alldone = 1;
+  __syncthreads();
+  const int it = init ? 0 : G->it + 1;
+  if (threadIdx.x < KR) {
+    const int jj = threadIdx.x;
+    ColState& c = cs[jj];
+    double a = 0.0, b = 0.0, s = 0.0, q = 0.0;
+    for (int blk = 0; blk < (int)gridDim.x; ++blk) {
+      const double* o = part + ((size_t)blk * KR + jj) * 4;
+      a = fmax(a, __ldcg(o)); b = fmax(b, __ldcg(o + 1)); s += __ldcg(o + 2); q += __ldcg(o + 3);
+    }
+    if (init) {
+      if (c.active) {
+        c.rz = s; c.rr0 = q; c.rr = q; c.beta = 0.0; c.done = 0; c.failed = 0; c.iters = 0;
+      } else {
+        c.done = 1;
+      }
+    } else if (c.active && !c.done) {
+      c.maxp = a; c.maxu = b; c.rr = q;
+      bool stop = (G->mode == 0) ? (fabs(c.alpha) * a / b <= c.tol) : (q <= c.tol * c.tol * c.rr0);
+      if (stop) {
+        c.done = 1; c.iters = it;
+      } else if (it >= G->maxiter) {
+        c.done = 1; c.failed = 1; c.iters = G->maxiter + 1;
+      } else {
+        c.beta = s / c.rz;
+        c.rz = s;
+      }
+    }
+    if (jj < G->kcols && c.active && !c.done) atomicAnd(&s_alldone, 0);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    G->it = it;
+    G->all_done = s_alldone;
+    G->cntC = 0;
+  }
+}
+
+template <typename V, int KR>
+void pcg_update(int n1, V* u, V* r, V* z, const V* p, const V* kp, const V* f, const V* dprecon, int init,
+                ColState* cs, PcgGlobal* G, double* part, cudaStream_t s) {
+  k_pcg_update<V, KR><<<NPART, RED_THREADS, 0, s>>>(n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
+}
+
+// ---------------------------------------------------------------------------
+// K5: one stress / yield / flow / body-load pass for one trial.
+// One warp per element, lane i < 27 = GLL point i.  Mirrors src/slope.F90:311-383:
+// eps = B x_e - evpt; sigma = C eps; eff = sigma + stress; invariants
+// (stress_invariant), F (mohcouf); if F >= 0: dQ (mohcouq), M1..M3 (formm),
+// flow = F (M1 dq1 + M2 dq2 + M3 dq3), evp = flow eff dt, evpt += evp and,
+// unless finalising, bload += B^T (C evp) detJ w; when finalising, stress = eff.
+// Yb receives the element body-load vector (zeros when finalising), to be
+// gathered in element order into bodyload.
+// ---------------------------------------------------------------------------
+constexpr int STRESS_WARPS = 4;
+constexpr double DEG2RAD_D = 3.141592653589793 / 180.0;
+
+__device__ __forceinline__ void stress_invariant_d(const double* s, double& sigm, double& dsbar, double& theta) {
+  const double small = 1.e-12, three = 3.0, six = 6.0;
+  const double sq3 = sqrt(three);
+  double s1 = s[0], s2 = s[1], s3 = s[2], s4 = s[3], s5 = s[4], s6 = s[5];
+  sigm = (s1 + s2 + s3) / three;
+  double d2 = ((s1 - s2) * (s1 - s2) + (s2 - s3) * (s2 - s3) + (s3 - s1) * (s3 - s1)) / six + s4 * s4 + s5 * s5 +
+              s6 * s6;
+  if (d2 < small) d2 = small;
+  double ds1 = s1 - sigm, ds2 = s2 - sigm, ds3 = s3 - sigm;
+  double d3 = ds1 * ds2 * ds3 - ds1 * s5 * s5 - ds2 * s6 * s6 - ds3 * s4 * s4 + 2.0 * s4 * s5 * s6;
+  double sq = sqrt(d2);
+  dsbar = sq3 * sq;
+  if (dsbar < small) {
+    theta = 0.0;
+  } else {
+    double sine = -three * sq3 * d3 / (2.0 * (sq * sq * sq));
+    if (sine >= 1.0) sine = 1.0;
+    if (sine < -1.0) sine = -1.0;
+    theta = asin(sine) / three;
+  }
+}
+
+__global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
+    const double* __restrict__ geo, const int* __restrict__ elist, int nel, const int* __restrict__ ge,
+    const int* __restrict__ mat_id, const double* __restrict__ x, int xstride, int xcol, const MatF* __restrict__ mf,
+    double dt, int nl_isconv, int finalize, double* __restrict__ evpt, double* __restrict__ stress,
+    double* __restrict__ Yb, int ystride, int ycol, double* __restrict__ fmax_part) {
+  __shared__ double s_eld[STRESS_WARPS][NEDOF];
+  __shared__ double s_q[STRESS_WARPS][NGLL][9];
+  __shared__ double s_fmax[STRESS_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool want_bload = !nl_isconv && !finalize;
+  double fmax_l = 0.0;
+  for (int le = blockIdx.x * STRESS_WARPS + warp; le < nel; le += gridDim.x * STRESS_WARPS) {
+    const int e = elist ? elist[le] : le;
+    const MatF m = mf[mat_id[e] - 1];
+    for (int t = lane; t < NEDOF; t += 32) s_eld[warp][t] = x[(size_t)ge[(size_t)e * NEDOF + t] * xstride + xcol];
+    __syncwarp();
+    if (lane < NGLL) {
+      const int i = lane;
+      const int ic[3] = {i % 3, (i / 3) % 3, i / 9};
+      const double* gp = geo + ((size_t)e * NGLL + i) * GEO_STRIDE;
+      double Ji[9];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) Ji[t] = gp[t];
+      const double detj = gp[9];
+      // du_c/dxi_a from the three nodes on the line through i along a
+      double dU[3][3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        int stride = (a == 0) ? 1 : (a == 1 ? 3 : 9);
+        int base = i - ic[a] * stride;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          double s = 0.0;
+#pragma unroll
+          for (int mm = 0; mm < 3; ++mm) s = s + c_D[ic[a]][mm] * s_eld[warp][3 * (base + mm * stride) + c];
+          dU[c][a] = s;
+        }
+      }
+      // G[c][d] = du_c/dx_d = sum_a Jinv(d,a) dU[c][a]
+      double Gm[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) Gm[c][d] = Ji[3 * d] * dU[c][0] + Ji[3 * d + 1] * dU[c][1] + Ji[3 * d + 2] * dU[c][2];
+      double* ev = evpt + ((size_t)e * NGLL + i) * NST;
+      double* se = stress + ((size_t)e * NGLL + i) * NST;
+      double eps[6] = {Gm[0][0], Gm[1][1], Gm[2][2], Gm[0][1] + Gm[1][0], Gm[1][2] + Gm[2][1], Gm[2][0] + Gm[0][2]};
+      double evl[6];
+#pragma unroll
+      for (int s = 0; s < 6; ++s) { evl[s] = ev[s]; eps[s] = eps[s] - evl[s]; }
+      double sig[6];
+      sig[0] = m.c11 * eps[0] + m.c12 * eps[1] + m.c12 * eps[2];
+      sig[1] = m.c12 * eps[0] + m.c11 * eps[1] + m.c12 * eps[2];
+      sig[2] = m.c12 * eps[0] + m.c12 * eps[1] + m.c11 * eps[2];
+      sig[3] = m.c44 * eps[3]; sig[4] = m.c44 * eps[4]; sig[5] = m.c44 * eps[5];
+      double eff[6];
+#pragma unroll
+      for (int s = 0; s < 6; ++s) eff[s] = sig[s] + se[s];
+      double sigm, dsbar, theta;
+      stress_invariant_d(eff, sigm, dsbar, theta);
+      double snth, csth;
+      sincos(theta, &snth, &csth);
+      const double r3 = 3.0, sq3 = sqrt(3.0);
+      // mohcouf (src/plastic_library.f90:95-108)
+      double f = m.snph * sigm + dsbar * (csth / sq3 - snth * m.snph / r3) - m.cohf * m.csph;
+      fmax_l = fmax(fmax_l, f);
+      double q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      if (f >= 0.0) {
+        // mohcouq (src/plastic_library.f90:116-143)
+        double dq1 = m.snps, dq2, dq3;
+        if (fabs(snth) > 0.49) {
+          double c1 = snth < 0.0 ? -1.0 : 1.0;
+          dq2 = (sq3 * 0.5 - c1 * m.snps * 0.5 / sq3) * sq3 * 0.5 / dsbar;
+          dq3 = 0.0;
+        } else {
+          double cs3th = cos(r3 * theta), tn3th = tan(r3 * theta), tnth = snth / csth;
+          dq2 = sq3 * csth / dsbar * ((1.0 + tnth * tn3th) + m.snps * (tn3th - tnth) / sq3) * 0.5;
+          dq3 = 0.5 * r3 * (sq3 * snth + m.snps * csth) / (cs3th * dsbar * dsbar);
+        }
+        // formm (src/plastic_library.f90:150-208): M1, M2, M3 (divided by 3)
+        const double sx = eff[0], sy = eff[1], sz = eff[2], txy = eff[3], tyz = eff[4], tzx = eff[5];
+        const double sgm = (sx + sy + sz) / r3;
+        const double dx = sx - sgm, dy = sy - sgm, dz = sz - sgm;
+        double M[6][6];
+        const double m1v = 1.0 / (r3 * sgm) / r3;
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+          for (int b = 0; b < 6; ++b) M[a][b] = 0.0;
+        double m3[6][6];
+        m3[0][0] = dx; m3[0][1] = dz; m3[0][2] = dy; m3[0][3] = txy; m3[0][4] = -2.0 * tyz; m3[0][5] = tzx;
+        m3[1][1] = dy; m3[1][2] = dx; m3[1][3] = txy; m3[1][4] = tyz; m3[1][5] = -2.0 * tzx;
+        m3[2][2] = dz; m3[2][3] = -2.0 * txy; m3[2][4] = tyz; m3[2][5] = tzx;
+        m3[3][3] = -r3 * dz; m3[3][4] = r3 * tzx; m3[3][5] = r3 * tyz;
+        m3[4][4] = -r3 * dx; m3[4][5] = r3 * txy;
+        m3[5][5] = -r3 * dy;
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+          for (int b = a; b < 6; ++b) {
+            double m1 = (a < 3 && b < 3) ? m1v : 0.0;
+            double m2 = 0.0;
+            if (a == b) m2 = (a < 3 ? 2.0 : 6.0) / r3;
+            else if (b < 3) m2 = -1.0 / r3;
+            double v = f * (m1 * dq1 + m2 * dq2 + (m3[a][b] / r3) * dq3);
+            M[a][b] = v;
+            M[b][a] = v;
+          }
+        double evp[6];
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+          double s = 0.0;
+#pragma unroll
+          for (int b = 0; b < 6; ++b) s = s + M[a][b] * eff[b];
+          evp[a] = s * dt;
+          ev[a] = evl[a] + evp[a];
+        }
+        if (want_bload) {
+          double dv[6];
+          dv[0] = m.c11 * evp[0] + m.c12 * evp[1] + m.c12 * evp[2];
+          dv[1] = m.c12 * evp[0] + m.c11 * evp[1] + m.c12 * evp[2];
+          dv[2] = m.c12 * evp[0] + m.c12 * evp[1] + m.c11 * evp[2];
+          dv[3] = m.c44 * evp[3]; dv[4] = m.c44 * evp[4]; dv[5] = m.c44 * evp[5];
+          const double S[3][3] = {{dv[0], dv[3], dv[5]}, {dv[3], dv[1], dv[4]}, {dv[5], dv[4], dv[2]}};
+          const double wd = detj * c_w[i];
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+              q[3 * c + a] = (S[c][0] * Ji[a] + S[c][1] * Ji[3 + a] + S[c][2] * Ji[6 + a]) * wd;
+        }
+      }
+      if (finalize) {
+#pragma unroll
+        for (int s = 0; s < 6; ++s) se[s] = eff[s];
+      }
+#pragma unroll
+      for (int t = 0; t < 9; ++t) s_q[warp][i][t] = q[t];
+    }
+    __syncwarp();
+    if (Yb && lane < NGLL) {
+      // node n = lane: F_n[c] = sum over points i on the lines through n, in
+      // increasing i, of sum_a Q_i[c][a] * dlagrange(a,i,n)
+      const int n = lane;
+      const int nc[3] = {n % 3, (n / 3) % 3, n / 9};
+      double F[3] = {0.0, 0.0, 0.0};
+      for (int i = 0; i < NGLL; ++i) {
+        const int ic[3] = {i % 3, (i / 3) % 3, i / 9};
+        int ndiff = (ic[0] != nc[0]) + (ic[1] != nc[1]) + (ic[2] != nc[2]);
+        if (ndiff > 1) continue;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          bool ok = true;
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+            if (b != a && ic[b] != nc[b]) ok = false;
+          if (!ok) continue;
+          double dl = c_D[ic[a]][nc[a]];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) F[c] = F[c] + s_q[warp][i][3 * c + a] * dl;
+        }
+      }
+      double* yo = Yb + ((size_t)le * NEDOF + 3 * n) * ystride + ycol;
+      yo[0] = F[0]; yo[ystride] = F[1]; yo[2 * ystride] = F[2];
+    }
+    __syncwarp();
+  }
+  // fmax partial per block
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) fmax_l = fmax(fmax_l, __shfl_xor_sync(FULL, fmax_l, o));
+  if (lane == 0) s_fmax[warp] = fmax_l;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int w = 0; w < STRESS_WARPS; ++w) v = fmax(v, s_fmax[w]);
+    fmax_part[blockIdx.x] = v;
+  }
+}
+
+void launch_stress_update(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
+                          const double* x, int xstride, int xcol, const MatF* mf, double dt, int nl_isconv,
+                          int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
+                          double* fmax_part, cudaStream_t s) {
+  // fixed grid so that fmax_part has NPART entries
+  k_stress_update<<<NPART, STRESS_WARPS * 32, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, xstride, xcol, mf, dt,
+                                                       nl_isconv, finalize, evpt, stress, Yb, ystride, ycol,
+                                                       fmax_part);
+}
+
+// elastic_stress (src/postprocess.f90:40-79): sigma = C B x per GLL point
+// (accumulate = 1 adds to the existing stress, the elastic_stress_intact form).
+__global__ void k_elastic_stress(const double* __restrict__ geo, const int* __restrict__ elist, int nel,
+                                 const int* __restrict__ ge, const int* __restrict__ mat_id,
+                                 const double* __restrict__ x, const MatF* __restrict__ mf, int accumulate,
+                                 double* __restrict__ stress) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nel * NGLL) return;
+  int le = t / NGLL, i = t - le * NGLL;
+  int e = elist ? elist[le] : le;
+  const MatF m = mf[mat_id[e] - 1];
+  const int ic[3] = {i % 3, (i / 3) % 3, i / 9};
+  const double* gp = geo + ((size_t)e * NGLL + i) * GEO_STRIDE;
+  const int* g = ge + (size_t)e * NEDOF;
+  double dU[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    int stride = (a == 0) ? 1 : (a == 1 ? 3 : 9);
+    int base = i - ic[a] * stride;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double s = 0.0;
+#pragma unroll
+      for (int mm = 0; mm < 3; ++mm) s = s + c_D[ic[a]][mm] * x[g[3 * (base + mm * stride) + c]];
+      dU[c][a] = s;
+    }
+  }
+  double Gm[3][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) Gm[c][d] = gp[3 * d] * dU[c][0] + gp[3 * d + 1] * dU[c][1] + gp[3 * d + 2] * dU[c][2];
+  double eps[6] = {Gm[0][0], Gm[1][1], Gm[2][2], Gm[0][1] + Gm[1][0], Gm[1][2] + Gm[2][1], Gm[2][0] + Gm[0][2]};
+  double sig[6];
+  sig[0] = m.c11 * eps[0] + m.c12 * eps[1] + m.c12 * eps[2];
+  sig[1] = m.c12 * eps[0] + m.c11 * eps[1] + m.c12 * eps[2];
+  sig[2] = m.c12 * eps[0] + m.c12 * eps[1] + m.c11 * eps[2];
+  sig[3] = m.c44 * eps[3]; sig[4] = m.c44 * eps[4]; sig[5] = m.c44 * eps[5];
+  double* se = stress + ((size_t)e * NGLL + i) * NST;
+#pragma unroll
+  for (int s = 0; s < 6; ++s) se[s] = accumulate ? se[s] + sig[s] : sig[s];
+}
+
+void launch_elastic_stress(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
+                           const double* x, const MatF* mf, int accumulate, double* stress, cudaStream_t s) {
+  int n = nel * NGLL;
+  if (n > 0) k_elastic_stress<<<(n + 127) / 128, 128, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, mf, accumulate,
+                                                              stress);
+}
+
+// overburden_stress (src/postprocess.f90:10-33)
+__global__ void k_overburden(const double* __restrict__ g_coord, const int* __restrict__ g_num,
+                             const int* __restrict__ mat_id, const double* __restrict__ gam, int nelmt, double z0,
+                             double p0, double k0, double* __restrict__ stress) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nelmt * NGLL) return;
+  int e = t / NGLL;
+  double z = g_coord[(size_t)3 * g_num[t] + 2];
+  double szz = p0 - gam[mat_id[e] - 1] * fabs(z - z0);
+  double* s = stress + (size_t)t * NST;
+  s[2] = szz; s[0] = k0 * szz; s[1] = k0 * szz;
+}
+
+void launch_overburden(const double* g_coord, const int* g_num, const int* mat_id, const double* gam, int nelmt,
+                       double z0, double p0, double k0, double* stress, cudaStream_t s) {
+  int n = nelmt * NGLL;
+  if (n > 0) k_overburden<<<(n + 255) / 256, 256, 0, s>>>(g_coord, g_num, mat_id, gam, nelmt, z0, p0, k0, stress);
+}
+
+// K9: equivalent nodal load of removed elements, sum_i B_i^T sigma_i detJ w
+// plus gamma detJ w on the z dof of node i (excavation_load_nodal,
+// src/excavation_library.f90:186-236).  One thread per (element, node).
+__global__ void k_release_load(const double* __restrict__ geo, const int* __restrict__ elist, int nel,
+                               const int* __restrict__ mat_id, const double* __restrict__ gam,
+                               const double* __restrict__ stress, double* __restrict__ Ye) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nel * NGLL) return;
+  int le = t / NGLL, n = t - le * NGLL;
+  int e = elist[le];
+  double F[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < NGLL; ++i) {
+    if (!on_line(i, n)) continue;
+    const double* gp = geo + ((size_t)e * NGLL + i) * GEO_STRIDE;
+    double g[3];
+    point_grad(gp, i, n, g);
+    const double* sg = stress + ((size_t)e * NGLL + i) * NST;
+    double wd = gp[9] * c_w[i];
+    F[0] = F[0] + (sg[0] * g[0] + sg[3] * g[1] + sg[5] * g[2]) * wd;
+    F[1] = F[1] + (sg[1] * g[1] + sg[3] * g[0] + sg[4] * g[2]) * wd;
+    F[2] = F[2] + (sg[2] * g[2] + sg[4] * g[1] + sg[5] * g[0]) * wd;
+  }
+  const double* gn = geo + ((size_t)e * NGLL + n) * GEO_STRIDE;
+  double eld = gn[9] * c_w[n];
+  double* yo = Ye + (size_t)le * NEDOF + 3 * n;
+  yo[0] = F[0];
+  yo[1] = F[1];
+  yo[2] = eld * gam[mat_id[e] - 1] + F[2];
+}
+
+void launch_release_load(const double* geo, const int* elist, int nel, const int* mat_id, const double* gam,
+                         const double* stress, double* Ye, cudaStream_t s) {
+  int n = nel * NGLL;
+  if (n > 0) k_release_load<<<(n + 127) / 128, 128, 0, s>>>(geo, elist, nel, mat_id, gam, stress, Ye);
+}
+
+// ---------------------------------------------------------------------------
+// Small vector kernels with per-column reductions written to part[NPART][KR][q].
+// ---------------------------------------------------------------------------
+// K8 nl check (src/slope.F90:307-309): max|x-oldx|, max|x| per column, oldx = x.
+__global__ void k_nl_check(int n1, int KR, const double* __restrict__ x, double* __restrict__ oldx,
+                           double* __restrict__ part) {
+  __shared__ double s[RED_THREADS][2];
+  double a = 0.0, b = 0.0;
+  const int j = threadIdx.x % KR;
+  const size_t n = (size_t)n1 * KR;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double xi = x[i];
+    a = fmax(a, fabs(xi - oldx[i]));
+    b = fmax(b, fabs(xi));
+    oldx[i] = xi;
+  }
+  s[threadIdx.x][0] = a;
+  s[threadIdx.x][1] = b;
+  __syncthreads();
+  if (threadIdx.x < KR) {
+    double A = 0.0, B = 0.0;
+    for (int t = threadIdx.x; t < RED_THREADS; t += KR) { A = fmax(A, s[t][0]); B = fmax(B, s[t][1]); }
+    part[((size_t)blockIdx.x * KR + j) * 2] = A;
+    part[((size_t)blockIdx.x * KR + j) * 2 + 1] = B;
+  }
+}
+
+void launch_nl_check(int n1, int KR, int k, const double* x, double* oldx, double* part, cudaStream_t s) {
+  (void)k;
+  k_nl_check<<<NPART, RED_THREADS, 0, s>>>(n1, KR, x, oldx, part);
+}
+
+// load = extload + bodyload; load(0) = 0 (src/slope.F90:288-289)
+__global__ void k_load_combine(int n1, int KR, const double* __restrict__ ext, const double* __restrict__ body,
+                               double* __restrict__ load) {
+  size_t n = (size_t)n1 * KR;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    size_t row = i / KR;
+    load[i] = row == 0 ? 0.0 : ext[row] + body[i];
+  }
+}
+
+void launch_load_combine(int n1, int KR, const double* extload, const double* bodyload, double* load,
+                         cudaStream_t s) {
+  k_load_combine<<<NPART, RED_THREADS, 0, s>>>(n1, KR, extload, bodyload, load);
+}
+
+// r64 = f - kp (FP64), r32 = (float) r64; partials |r|^2, |f|^2 per column.
+__global__ void k_residual(int n1, int KR, const double* __restrict__ f, const double* __restrict__ kp,
+                           double* __restrict__ r64, float* __restrict__ r32, double* __restrict__ part) {
+  __shared__ double s[RED_THREADS][2];
+  double a = 0.0, b = 0.0;
+  const int j = threadIdx.x % KR;
+  const size_t n = (size_t)n1 * KR;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double ri = (i < (size_t)KR) ? 0.0 : f[i] - kp[i];
+    r64[i] = ri;
+    r32[i] = (float)ri;
+    a += ri * ri;
+    b += f[i] * f[i];
+  }
+  s[threadIdx.x][0] = a;
+  s[threadIdx.x][1] = b;
+  __syncthreads();
+  if (threadIdx.x < KR) {
+    double A = 0.0, B = 0.0;
+    for (int t = threadIdx.x; t < RED_THREADS; t += KR) { A += s[t][0]; B += s[t][1]; }
+    part[((size_t)blockIdx.x * KR + j) * 2] = A;
+    part[((size_t)blockIdx.x * KR + j) * 2 + 1] = B;
+  }
+}
+
+void launch_residual_norms(int n1, int KR, const double* f, const double* kp, double* r64, float* r32,
+                           double* part, cudaStream_t s) {
+  k_residual<<<NPART, RED_THREADS, 0, s>>>(n1, KR, f, kp, r64, r32, part);
+}
+
+// x += d for the columns in colmask; partials max|d|, max|x| per column.
+__global__ void k_axpy_corr(int n1, int KR, const int* __restrict__ colmask, const float* __restrict__ d,
+                            double* __restrict__ x, double* __restrict__ part) {
+  __shared__ double s[RED_THREADS][2];
+  double a = 0.0, b = 0.0;
+  const int j = threadIdx.x % KR;
+  const bool on = colmask[j] != 0;
+  const size_t n = (size_t)n1 * KR;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double xi = x[i];
+    if (on) {
+      double di = (double)d[i];
+      xi = xi + di;
+      x[i] = xi;
+      a = fmax(a, fabs(di));
+    }
+    b = fmax(b, fabs(xi));
+  }
+  s[threadIdx.x][0] = a;
+  s[threadIdx.x][1] = b;
+  __syncthreads();
+  if (threadIdx.x < KR) {
+    double A = 0.0, B = 0.0;
+    for (int t = threadIdx.x; t < RED_THREADS; t += KR) { A = fmax(A, s[t][0]); B = fmax(B, s[t][1]); }
+    part[((size_t)blockIdx.x * KR + j) * 2] = A;
+    part[((size_t)blockIdx.x * KR + j) * 2 + 1] = B;
+  }
+}
+
+void launch_axpy_correction(int n1, int KR, const int* colmask, const float* d, double* x, double* part,
+                            cudaStream_t s) {
+  k_axpy_corr<<<NPART, RED_THREADS, 0, s>>>(n1, KR, colmask, d, x, part);
+}
+
+// dprecon(1:) = 1/dprecon(1:), dprecon(0) = 0 (src/slope.F90:199), plus an FP32 copy.
+__global__ void k_invert_diag(int n1, double* __restrict__ dp, float* __restrict__ dp32) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n1) return;
+  double v = (i == 0) ? 0.0 : 1.0 / dp[i];
+  dp[i] = v;
+  if (dp32) dp32[i] = (float)v;
+}
+
+void launch_invert_diag(int n1, double* dprecon, float* dprecon32, cudaStream_t s) {
+  k_invert_diag<<<(n1 + 255) / 256, 256, 0, s>>>(n1, dprecon, dprecon32);
+}
+
+// explicit instantiations
+#define SG_INST(V, KR)                                                                                          \
+  template void pcg_apply<V, KR>(int, const void*, const int*, int, const V*, const V*, int, V*, const ColState*, \
+                                 const PcgGlobal*, const int*, cudaStream_t);                                   \
+  template void pcg_gather<V, KR>(const GatherTopo&, const V*, V*, V*, const V*, int, ColState*, PcgGlobal*,    \
+                                  double*, cudaStream_t);                                                       \
+  template void pcg_update<V, KR>(int, V*, V*, V*, const V*, const V*, const V*, const V*, int, ColState*,      \
+                                  PcgGlobal*, double*, cudaStream_t);
+SG_INST(double, 1)
+SG_INST(double, 2)
+SG_INST(double, 4)
+SG_INST(double, 8)
+SG_INST(double, 16)
+SG_INST(float, 1)
+SG_INST(float, 2)
+SG_INST(float, 4)
+SG_INST(float, 8)
+SG_INST(float, 16)
+template void launch_gather_plain<double>(const GatherTopo&, int, const double*, double*, int, const int*,
+                                          cudaStream_t);
+template void launch_gather_plain<float>(const GatherTopo&, int, const float*, float*, int, const int*,
+                                         cudaStream_t);
+
+// Fixed-order reduction of block partials part[nblk][KR][nq] into out[KR][nq];
+// bit q of maxmask selects max instead of sum for quantity q.
+__global__ void k_final_reduce(const double* __restrict__ part, int nblk, int KR, int nq, int maxmask,
+                               double* __restrict__ out) {
+  int t = threadIdx.x;
+  if (t >= KR * nq) return;
+  int q = t % nq;
+  bool mx = (maxmask >> q) & 1;
+  double v = 0.0;
+  for (int b = 0; b < nblk; ++b) {
+    double x = part[(size_t)b * KR * nq + t];
+    v = mx ? fmax(v, x) : v + x;
+  }
+  out[t] = v;
+}
+
+void launch_final_reduce(const double* part, int nblk, int KR, int nq, int maxmask, double* out, cudaStream_t s) {
+  k_final_reduce<<<1, 128, 0, s>>>(part, nblk, KR, nq, maxmask, out);
+}
+
+// Nodal displacement maxima of one column (src/slope.F90:400-415):
+// part[b][0] = max |u_d| over nodes and dofs, part[b][1] = max |u| (node norm).
+__global__ void k_disp_max(int nnode, const int* __restrict__ gdof, const double* __restrict__ x, int KR, int col,
+                           double* __restrict__ part) {
+  __shared__ double s[RED_THREADS][2];
+  double a = 0.0, b = 0.0;
+  for (int nd = blockIdx.x * blockDim.x + threadIdx.x; nd < nnode; nd += gridDim.x * blockDim.x) {
+    double u[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      int g = gdof[3 * nd + d];
+      u[d] = g ? x[(size_t)g * KR + col] : 0.0;
+      a = fmax(a, fabs(u[d]));
+    }
+    b = fmax(b, sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+  }
+  s[threadIdx.x][0] = a;
+  s[threadIdx.x][1] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double A = 0.0, B = 0.0;
+    for (int t = 0; t < RED_THREADS; ++t) { A = fmax(A, s[t][0]); B = fmax(B, s[t][1]); }
+    part[2 * blockIdx.x] = A;
+    part[2 * blockIdx.x + 1] = B;
+  }
+}
+
+void launch_disp_max(int nnode, const int* gdof, const double* x, int KR, int col, double* part, cudaStream_t s) {
+  k_disp_max<<<NPART, RED_THREADS, 0, s>>>(nnode, gdof, x, KR, col, part);
+}
+
+// x(:,col) /= n etc.: y[i*KR+col] = a*y[i*KR+col] (all columns when col < 0)
+__global__ void k_scale(size_t n, double* __restrict__ y, double a) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) y[i] = y[i] / a;
+}
+void launch_div(size_t n, double* y, double a, cudaStream_t s) { k_scale<<<NPART, RED_THREADS, 0, s>>>(n, y, a); }
+
+}  // namespace sg

@@ -1,0 +1,79 @@
+// sg_kernels.cuh -- device-side declarations shared by the kernel and driver
+// translation units.
+#pragma once
+
+#include "sg_internal.h"
+
+namespace sg {
+
+// Per right-hand-side column PCG scalars (device resident).
+struct ColState {
+  double rz;      // r.z of the current iterate
+  double alpha;   // step length of this iteration
+  double beta;    // direction update factor for the next iteration
+  double tol;     // stop tolerance (step test) or residual reduction (residual test)
+  double rr0;     // |r0|^2 at the start (residual test)
+  double maxp, maxu, rr;  // last evaluated max|p|, max|u|, |r|^2
+  int active;     // column takes part in this solve
+  int done;       // stop test met (or failed)
+  int iters;      // iteration at which the column stopped
+  int failed;     // reached maxiter without meeting the test
+};
+
+// Global PCG control word (device resident).
+struct PcgGlobal {
+  int all_done;
+  int it;         // iterations completed
+  int maxiter;
+  int mode;       // 0 = reference step test, 1 = residual reduction test
+  int kcols;      // columns in use (<= KR)
+  unsigned cntB, cntC, pad;
+};
+
+// Factored material block for the stress update, per trial.
+struct MatF {
+  double c11, c12, c44;  // compute_cmat(ym, nuf) entries (src/elastic.f90:13-42)
+  double snph, csph;     // sin, cos of phif (mohcouf, src/plastic_library.f90:95-108)
+  double cohf;
+  double snps;           // sin of psif (mohcouq, src/plastic_library.f90:116-143)
+  double pad;
+};
+
+// Kernel launch wrappers (sg_kernels.cu)
+template <typename V, int KR>
+void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_old, const V* z, int combine,
+               V* Y, const ColState* cs, const PcgGlobal* G, const int* d_nbr, cudaStream_t s);
+template <typename V, int KR>
+void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mode, ColState* cs,
+                PcgGlobal* G, double* part, cudaStream_t s);
+template <typename V, int KR>
+void pcg_update(int n1, V* u, V* r, V* z, const V* p, const V* kp, const V* f, const V* dprecon, int init,
+                ColState* cs, PcgGlobal* G, double* part, cudaStream_t s);
+
+// Yb layout [nel][81][ystride] at column ycol (ystride = KR of the trial batch)
+void launch_stress_update(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
+                          const double* x, int xstride, int xcol, const MatF* mf, double dt, int nl_isconv,
+                          int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
+                          double* fmax_part, cudaStream_t s);
+void launch_elastic_stress(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
+                           const double* x, const MatF* mf, int accumulate, double* stress, cudaStream_t s);
+void launch_overburden(const double* g_coord, const int* g_num, const int* mat_id, const double* gam, int nelmt,
+                       double z0, double p0, double k0, double* stress, cudaStream_t s);
+void launch_release_load(const double* geo, const int* elist, int nel, const int* mat_id, const double* gam,
+                         const double* stress, double* Ye, cudaStream_t s);
+void launch_nl_check(int n1, int KR, int k, const double* x, double* oldx, double* part, cudaStream_t s);
+void launch_load_combine(int n1, int KR, const double* extload, const double* bodyload, double* load,
+                         cudaStream_t s);
+template <typename V>
+void launch_gather_plain(const GatherTopo& T, int KR, const V* Y, V* out, int accumulate, const int* colmask,
+                         cudaStream_t s);
+void launch_final_reduce(const double* part, int nblk, int KR, int nq, int maxmask, double* out, cudaStream_t s);
+void launch_disp_max(int nnode, const int* gdof, const double* x, int KR, int col, double* part, cudaStream_t s);
+void launch_div(size_t n, double* y, double a, cudaStream_t s);
+void launch_residual_norms(int n1, int KR, const double* f, const double* kp, double* r64, float* r32,
+                           double* part, cudaStream_t s);
+void launch_axpy_correction(int n1, int KR, const int* colmask, const float* d, double* x, double* part,
+                            cudaStream_t s);
+void launch_invert_diag(int n1, double* dprecon, float* dprecon32, cudaStream_t s);
+
+}  // namespace sg

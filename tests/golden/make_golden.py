@@ -1,0 +1,60 @@
+"""Generate the committed golden fixtures under tests/golden/ with the CPU oracle.
+
+The reference (Fortran) cannot be compiled on the build machines, so long
+oracle runs whose results the GPU tests compare against are stored here as
+small JSON files instead of being recomputed in every test session.
+
+    python tests/golden/make_golden.py slope2d_sweep     # ~20-40 min, 1 core
+    python tests/golden/make_golden.py slope2d_trials    # ~1 min
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.pyoracle import OracleModel  # noqa: E402
+from specfem3d_geotech_gb300 import meshgen  # noqa: E402
+
+
+def slope2d_sweep():
+    """The 300-element slope's SRF sweep 1.00:0.05:2.00 up to the first failure."""
+    m = meshgen.slope2d()
+    om = OracleModel(m)
+    t0 = time.time()
+    rows = []
+    for s in m.control.srf:
+        r = om.trial(s)
+        r["seconds"] = time.time() - t0
+        rows.append(r)
+        print(json.dumps(r), flush=True)
+        if r["failed"] or r["errcode"]:
+            break
+    crit = next((r["srf"] for r in rows if r["failed"]), None)
+    out = dict(mesh="slope2d", nelmt=om.nelmt, neq=om.neq, control=m.control.__dict__, trials=rows,
+               critical_srf=crit, oracle_seconds=time.time() - t0)
+    with open(os.path.join(HERE, "slope2d_sweep.json"), "w") as f:
+        json.dump(out, f, indent=1, default=list)
+
+
+def slope2d_trials():
+    """Per-trial summaries and per-NL-iteration PCG counts at SRF 1.0 and 1.1."""
+    m = meshgen.slope2d()
+    om = OracleModel(m)
+    rows = []
+    for s in (1.0, 1.1):
+        r = om.trial(s, want_log=True)
+        r["nl_cg"] = r["nl_cg"].tolist()
+        rows.append(r)
+    with open(os.path.join(HERE, "slope2d_trials.json"), "w") as f:
+        json.dump(dict(mesh="slope2d", trials=rows), f, indent=1)
+
+
+if __name__ == "__main__":
+    for name in sys.argv[1:]:
+        globals()[name]()

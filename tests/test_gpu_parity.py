@@ -1,0 +1,179 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Tolerances: the FP64 path must match the oracle's displacement to relative
+L2 <= 1e-9 with identical plastic-iteration counts; the mixed FP32/FP64
+refinement form must stay within 1e-6 of the FP64 result.  Integer outputs
+(node numbering, dof maps) must be identical.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import specfem3d_geotech_gb300 as sg
+from oracle.pyoracle import OracleModel, pcg_solver as orc_pcg
+from specfem3d_geotech_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-9
+MIXED_TOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def slope():
+    mesh = meshgen.slope2d()
+    return mesh, OracleModel(mesh)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_dropin_pcg_matches_oracle(ctx, slope):
+    mesh, om = slope
+    km, dp, ext = om.stiffness_bodyload()
+    dinv = np.where(np.arange(om.neq + 1) > 0, 1.0 / np.where(dp == 0, 1, dp), 0.0)
+    ge = om.arrays()["gdof_elmt"]
+    u_ref = np.zeros(om.neq + 1)
+    err_r, it_r = orc_pcg(om.neq, om.nelmt, km, u_ref, ext, dinv, ge, 5000, 1e-8)
+    u = np.zeros(om.neq + 1)
+    it, err, tag = sg.pcg_solver(om.neq, om.nelmt, km, u, ext, dinv, ge, 5000, 1e-8, ctx=ctx)
+    assert err == 0 and err_r == 0 and tag == ""
+    assert abs(it - it_r) <= 2
+    assert rel(u, u_ref) <= FP64_TOL
+    # warm start from a perturbed solution (src/solver.f90:38-46)
+    u0 = u_ref * 0.9
+    u1, u2 = u0.copy(), u0.copy()
+    err_r, it_r = orc_pcg(om.neq, om.nelmt, km, u1, ext, dinv, ge, 5000, 1e-8)
+    it, err, _ = sg.pcg_solver(om.neq, om.nelmt, km, u2, ext, dinv, ge, 5000, 1e-8, ctx=ctx)
+    assert err == 0 and abs(it - it_r) <= 2 and rel(u2, u1) <= FP64_TOL
+
+
+def test_dropin_nonconvergence_is_reported(ctx, slope):
+    mesh, om = slope
+    km, dp, ext = om.stiffness_bodyload()
+    dinv = np.where(np.arange(om.neq + 1) > 0, 1.0 / np.where(dp == 0, 1, dp), 0.0)
+    ge = om.arrays()["gdof_elmt"]
+    u = np.zeros(om.neq + 1)
+    it, err, tag = sg.pcg_solver(om.neq, om.nelmt, km, u, ext, dinv, ge, 3, 1e-8, ctx=ctx)
+    assert err == sg.SG_ERR_NOCONV == -1
+    assert tag.strip() == "ERROR: PCG solver doesn't converge!"
+    assert it == 4  # the Fortran DO variable after cg_maxiter iterations
+
+
+def test_dropin_rejects_bad_dof_map(ctx, slope):
+    mesh, om = slope
+    km, dp, ext = om.stiffness_bodyload()
+    ge = om.arrays()["gdof_elmt"].copy()
+    ge[0, 0] = om.neq + 5
+    u = np.zeros(om.neq + 1)
+    with pytest.raises(sg.SgError):
+        sg.pcg_solver(om.neq, om.nelmt, km, u, ext, dp, ge, 10, 1e-8, ctx=ctx)
+
+
+def test_model_mesh_and_stiffness_match_oracle(ctx, slope):
+    mesh, om = slope
+    m = sg.Model(mesh, ctx=ctx)
+    a, b = m.arrays(), om.arrays()
+    assert m.nnode == om.nnode and m.neq == om.neq
+    for key in ("g_num", "gdof", "gdof_elmt"):
+        assert np.array_equal(a[key], b[key]), key
+    assert np.abs(a["g_coord"] - b["g_coord"]).max() <= 1e-12 * np.abs(b["g_coord"]).max()
+    km, dp, ext = m.stiffness()
+    kr, dr, er = om.stiffness_bodyload()
+    assert np.abs(km - kr).max() <= 1e-12 * np.abs(kr).max()
+    assert rel(dp, dr) <= 1e-13
+    assert rel(ext, er) <= 1e-13
+
+
+def test_trial_matches_oracle_fp64(ctx, slope):
+    mesh, om = slope
+    m = sg.Model(mesh, ctx=ctx)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=2000)
+    for srf in (1.0, 1.1):
+        (r,), x = m.trials([srf], ctl, want_x=True)
+        ro = om.trial(srf, want_x=True, want_stress=True)
+        assert r["nl_iter"] == ro["nl_iter"] and r["converged"] == ro["converged"] == 1
+        assert abs(r["cg_tot"] - ro["cg_tot"]) <= max(3, 0.01 * ro["cg_tot"])
+        assert rel(x[0], ro["x"]) <= FP64_TOL
+        st = m.last_stress(0)
+        assert np.abs(st - ro["stress"]).max() <= 1e-8 * np.abs(ro["stress"]).max()
+        for key in ("uxmax", "umax", "fmax"):
+            assert abs(r[key] - ro[key]) <= 1e-8 * max(abs(ro[key]), 1e-12), key
+
+
+def test_golden_sweep_prefix(ctx):
+    """The first trials of the committed 300-element sweep are reproduced."""
+    path = os.path.join(os.path.dirname(__file__), "golden", "slope2d_sweep.json")
+    with open(path) as f:
+        gold = json.load(f)
+    m = sg.Model(meshgen.slope2d(), ctx=ctx)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=2000)
+    for g in gold["trials"][:3]:
+        r = m.trials([g["srf"]], ctl)[0]
+        assert r["nl_iter"] == g["nl_iter"]
+        assert abs(r["umax"] - g["umax"]) <= 1e-8 * g["umax"]
+
+
+def test_deterministic_bitwise(ctx, slope):
+    mesh, _ = slope
+    m = sg.Model(mesh, ctx=ctx)
+    ctl = sg.make_control()
+    _, x1 = m.trials([1.05], ctl, want_x=True)
+    _, x2 = m.trials([1.05], ctl, want_x=True)
+    assert np.array_equal(x1, x2)
+
+
+def test_batched_trials_equal_single(ctx, slope):
+    mesh, _ = slope
+    m = sg.Model(mesh, ctx=ctx)
+    ctl = sg.make_control()
+    srfs = [1.0, 1.05, 1.1]
+    res, xb = m.trials(srfs, ctl, want_x=True)
+    for t, s in enumerate(srfs):
+        (r1,), x1 = m.trials([s], ctl, want_x=True)
+        assert res[t]["nl_iter"] == r1["nl_iter"]
+        assert rel(xb[t], x1[0]) <= FP64_TOL
+
+
+def test_mixed_precision_within_tolerance(ctx, slope):
+    mesh, om = slope
+    m64 = sg.Model(mesh, ctx=ctx)
+    m32 = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    c64 = sg.make_control()
+    c32 = sg.make_control(precision=sg.PREC_MIXED)
+    (r64,), x64 = m64.trials([1.0], c64, want_x=True)
+    (r32,), x32 = m32.trials([1.0], c32, want_x=True)
+    assert r32["nl_iter"] == r64["nl_iter"]
+    assert rel(x32[0], x64[0]) <= MIXED_TOL
+    assert r32["refine_steps"] >= r32["nl_iter"]
+
+
+def test_confined_column_exact_on_gpu(ctx):
+    E, nu, gam, H = 1e5, 0.3, 20.0, 4.0
+    mesh = meshgen.column(n=4, H=H, E=E, nu=nu, gam=gam)
+    m = sg.Model(mesh, ctx=ctx)
+    ctl = sg.make_control(cg_tol=1e-14, nl_maxiter=10, allelastic=1)
+    (r,), x = m.trials([1.0], ctl, want_x=True)
+    a = m.arrays()
+    Mmod = E * (1 - nu) / ((1 + nu) * (1 - 2 * nu))
+    z = a["g_coord"][:, 2]
+    g = a["gdof"][:, 2]
+    uz = np.where(g > 0, x[0][g], 0.0)
+    ex = -gam * (H * z - z * z / 2) / Mmod
+    assert np.abs(uz - ex).max() <= 1e-9 * np.abs(ex).max()
+
+
+def test_excavation_matches_oracle(ctx):
+    mesh = meshgen.excavation(nx=6, ny=6, nz=4, L=12.0, H=8.0, pit=4.0, lifts=2, lift_h=2.0)
+    om = OracleModel(mesh)
+    om.set_control(1e-8, 5000, 1e-4, 200)
+    ro = om.excavation(1, 8.0, 0.0, 0.5, [2, 3])
+    m = sg.Model(mesh, ctx=ctx)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=200)
+    r = m.excavation(ctl, 1, 8.0, 0.0, 0.5, [2, 3])
+    assert r.shape == ro.shape
+    assert np.array_equal(r[:, 2], ro[:, 2])            # plastic iterations per stage
+    assert np.allclose(r[:, 3:5], ro[:, 3:5], rtol=1e-8)  # uxmax, umax

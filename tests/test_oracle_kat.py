@@ -1,0 +1,179 @@
+"""Known-answer checks that pin the CPU oracle (no GPU).
+
+The reference ships no tests or golden outputs and cannot be compiled here,
+so the oracle is pinned by analytic answers: the NGLL=3 GLL tables, the
+element matrix's rigid-body null space and symmetry, the exact confined
+gravity column, stress invariants at the Lode corners and Mohr-Coulomb
+yield values computed by hand.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from oracle.pyoracle import OracleModel
+from specfem3d_geotech_gb300 import meshgen
+
+L = pyoracle.lib()
+
+
+def tables():
+    w = np.zeros(27)
+    dl = np.zeros(3 * 27 * 27)
+    ds = np.zeros(3 * 8 * 27)
+    gn = np.zeros(8, np.int32)
+    fc = np.zeros(54, np.int32)
+    L.orc_tables(w, dl, ds, gn, fc)
+    return w, dl.reshape(3, 27, 27), ds.reshape(3, 8, 27), gn, fc.reshape(6, 9)
+
+
+def test_gll_weights_and_derivatives():
+    w, dl, ds, gn, fc = tables()
+    w1 = np.array([1 / 3, 4 / 3, 1 / 3])
+    ref = np.einsum("k,j,i->kji", w1, w1, w1).reshape(-1)
+    assert np.allclose(w, ref, rtol=0, atol=1e-15)
+    assert abs(w.sum() - 8.0) < 1e-14  # volume of the reference cube
+    # derivative of the Lagrange basis sums to zero (partition of unity)
+    assert np.abs(dl.sum(axis=2)).max() < 1e-14
+    # d/dxi of the hex8 shape functions sums to zero at every GLL point
+    assert np.abs(ds.sum(axis=1)).max() < 1e-14
+    assert gn.tolist() == [0, 2, 8, 6, 18, 20, 26, 24]
+    # Exodus faces: 1 y-min, 2 x-max, 3 y-max, 4 x-min, 5 z-min, 6 z-max
+    assert fc[4].tolist() == list(range(9)) and fc[5].tolist() == list(range(18, 27))
+    assert fc[3].tolist() == [0, 3, 6, 9, 12, 15, 18, 21, 24]
+
+
+def test_cmat_closed_form():
+    c = np.zeros(36)
+    E, nu = 1e5, 0.3
+    L.orc_cmat(E, nu, c)
+    c = c.reshape(6, 6)
+    lam = E * nu / ((1 + nu) * (1 - 2 * nu))
+    mu = E / (2 * (1 + nu))
+    ref = np.zeros((6, 6))
+    ref[:3, :3] = lam
+    ref[np.arange(3), np.arange(3)] = lam + 2 * mu
+    ref[np.arange(3, 6), np.arange(3, 6)] = mu
+    assert np.allclose(c, ref, rtol=1e-14)
+
+
+def inv(s):
+    out = np.zeros(3)
+    L.orc_stress_invariant(np.asarray(s, np.float64), out)
+    return out
+
+
+def test_stress_invariants_corners():
+    # hydrostatic: J2 clamped to 1e-12, theta = asin(0)/3 = 0
+    sigm, dsbar, th = inv([-5, -5, -5, 0, 0, 0])
+    assert sigm == -5 and abs(dsbar - math.sqrt(3e-12)) < 1e-18 and th == 0.0
+    # one principal stress above two equal ones: sin(3 theta) = -1, theta = -30 deg
+    # (tension positive, Smith & Griffiths' convention)
+    sigm, dsbar, th = inv([-10, -20, -20, 0, 0, 0])
+    assert abs(sigm + 50 / 3) < 1e-12
+    assert abs(dsbar - 10.0) < 1e-12
+    assert abs(th + math.pi / 6) < 1e-7
+    # one principal stress below two equal ones: theta = +30 deg
+    sigm, dsbar, th = inv([-20, -10, -10, 0, 0, 0])
+    assert abs(th - math.pi / 6) < 1e-7
+    # pure shear: theta = 0
+    sigm, dsbar, th = inv([0, 0, 0, 7, 0, 0])
+    assert abs(th) < 1e-12 and abs(dsbar - math.sqrt(3) * 7) < 1e-12
+
+
+def test_mohr_coulomb_hand_values():
+    phi, c = 30.0, 10.0
+    sigm, dsbar, th = -20.0, 15.0, 0.1
+    f = L.orc_mohcouf(phi, c, sigm, dsbar, th)
+    sp, cp = math.sin(math.radians(phi)), math.cos(math.radians(phi))
+    ref = sp * sigm + dsbar * (math.cos(th) / math.sqrt(3) - math.sin(th) * sp / 3) - c * cp
+    assert abs(f - ref) < 1e-12
+    # potential derivatives: smooth branch and corner branch (|sin theta| > 0.49)
+    dq = np.zeros(3)
+    L.orc_mohcouq(0.0, 12.0, 0.2, dq)
+    assert dq[0] == 0.0 and dq[1] > 0 and dq[2] != 0.0
+    L.orc_mohcouq(10.0, 12.0, math.asin(0.5) + 1e-3, dq)
+    sq3 = math.sqrt(3)
+    sps = math.sin(math.radians(10.0))
+    assert dq[2] == 0.0
+    assert abs(dq[1] - (sq3 * 0.5 - sps * 0.5 / sq3) * sq3 * 0.5 / 12.0) < 1e-15
+    m = np.zeros(108)
+    L.orc_formm(np.array([-3.0, -2.0, -1.0, 0.5, 0.2, -0.1]), m)
+    m = m.reshape(3, 6, 6)
+    for a in m:
+        assert np.allclose(a, a.T, atol=0)
+
+
+def test_element_matrix_rigid_body_and_symmetry():
+    mesh = meshgen.slope2d()
+    om = OracleModel(mesh)
+    km, dp, ext = om.stiffness_bodyload()
+    arr = om.arrays()
+    K = km[7].T  # [row, col]
+    coords = arr["g_coord"][arr["g_num"][7]]
+    scale = np.abs(K).max()
+    assert np.abs(K - K.T).max() <= 1e-12 * scale
+    modes = []
+    for d in range(3):
+        v = np.zeros((27, 3)); v[:, d] = 1; modes.append(v.reshape(-1))
+    for a, b in ((0, 1), (1, 2), (2, 0)):
+        v = np.zeros((27, 3)); v[:, a] = -coords[:, b]; v[:, b] = coords[:, a]; modes.append(v.reshape(-1))
+    for v in modes:
+        assert np.abs(K @ v).max() <= 1e-10 * scale * np.abs(v).max()
+    ev = np.linalg.eigvalsh(0.5 * (K + K.T))
+    assert ev.min() >= -1e-10 * scale
+    assert (ev > 1e-8 * scale).sum() == 81 - 6
+    # GLL structural zeros: nodes differing in all three lattice indices
+    n, m = 0, 26
+    assert np.all(K[3 * n:3 * n + 3, 3 * m:3 * m + 3] == 0.0)
+
+
+def test_confined_gravity_column_exact():
+    """1x1xn column, laterally confined, base fixed: u_z(z) = -g(Hz - z^2/2)/M."""
+    E, nu, gam, H, n = 1e5, 0.3, 20.0, 4.0, 4
+    mesh = meshgen.column(n=n, H=H, E=E, nu=nu, gam=gam)
+    om = OracleModel(mesh)
+    r = om.trial(1.0, want_x=True, want_stress=True)
+    assert r["errcode"] == 0
+    arr = om.arrays()
+    M = E * (1 - nu) / ((1 + nu) * (1 - 2 * nu))
+    z = arr["g_coord"][:, 2]
+    uz_exact = -gam * (H * z - z * z / 2) / M
+    g = arr["gdof"][:, 2]
+    uz = np.where(g > 0, r["x"][g], 0.0)
+    assert np.abs(uz - uz_exact).max() <= 1e-9 * np.abs(uz_exact).max()
+    szz = r["stress"][..., 2]
+    zp = arr["g_coord"][arr["g_num"], 2]
+    assert np.abs(szz - (-gam * (H - zp))).max() <= 1e-8 * gam * H
+
+
+def test_golden_trials_reproduce():
+    """The committed oracle fixture for the 300-element slope is reproduced."""
+    path = os.path.join(os.path.dirname(__file__), "golden", "slope2d_trials.json")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated")
+    with open(path) as f:
+        gold = json.load(f)
+    om = OracleModel(meshgen.slope2d())
+    g = gold["trials"][0]
+    r = om.trial(g["srf"], want_log=True)
+    assert r["nl_iter"] == g["nl_iter"] and r["cg_tot"] == g["cg_tot"]
+    assert r["nl_cg"].tolist() == g["nl_cg"]
+    assert abs(r["umax"] - g["umax"]) <= 1e-12 * g["umax"]
+
+
+def test_golden_sweep_bracket():
+    path = os.path.join(os.path.dirname(__file__), "golden", "slope2d_sweep.json")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated")
+    with open(path) as f:
+        gold = json.load(f)
+    rows = gold["trials"]
+    assert rows[-1]["failed"] == 1 and all(r["failed"] == 0 for r in rows[:-1])
+    assert gold["critical_srf"] == rows[-1]["srf"]
+    # plastic iterations grow towards failure
+    nl = [r["nl_iter"] for r in rows[:-1]]
+    assert nl == sorted(nl)
