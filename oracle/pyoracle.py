@@ -39,6 +39,7 @@ def lib():
         L.orc_model_from_deck.restype = vp
         L.orc_model_from_deck.argtypes = [C.c_char_p]
         L.orc_free.argtypes = [vp]
+        L.orc_set_dot_order.argtypes = [i]
         L.orc_model_sizes.argtypes = [vp, _ip]
         L.orc_model_arrays.argtypes = [vp, vp, vp, vp, vp, vp]
         L.orc_model_control.argtypes = [vp, _dp, _ip, vp]

@@ -611,7 +611,21 @@ double maxabs(const double* v, int n1) {
   for (int i = 0; i < n1; ++i) m = std::max(m, std::fabs(v[i]));
   return m;
 }
+// Dot-product summation order: 0 = sequential (the reference's dot_product),
+// 1 = pairwise halving.  The second order exists only to measure how far
+// rounding alone moves a PCG solve (the parity noise floor); it is never the default.
+int g_dot_order = 0;
+double dot_pairwise(const double* a, const double* b, int n) {
+  if (n <= 8) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s = s + a[i] * b[i];
+    return s;
+  }
+  int h = n / 2;
+  return dot_pairwise(a, b, h) + dot_pairwise(a + h, b + h, n - h);
+}
 double dot(const double* a, const double* b, int n1) {
+  if (g_dot_order == 1) return dot_pairwise(a, b, n1);
   double s = 0.0;
   for (int i = 0; i < n1; ++i) s = s + a[i] * b[i];
   return s;
@@ -1065,6 +1079,7 @@ void* orc_model_from_deck(const char* path) {
 }
 
 void orc_free(void* h) { delete (OrcModel*)h; }
+void orc_set_dot_order(int order) { g_dot_order = order; }
 
 void orc_model_sizes(void* hv, int* out /* nnode nelmt neq nmatblk nsrf */) {
   OrcModel* h = (OrcModel*)hv;

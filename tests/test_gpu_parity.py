@@ -1,9 +1,13 @@
 """GPU parity: the CUDA path through the C ABI against the CPU oracle.
 
 Tolerances: the FP64 path must match the oracle's displacement to relative
-L2 <= 1e-9 with identical plastic-iteration counts; the mixed FP32/FP64
-refinement form must stay within 1e-6 of the FP64 result.  Integer outputs
-(node numbering, dof maps) must be identical.
+L2 <= 1e-8 (the PCG step tolerance) with identical plastic-iteration counts.
+1e-8 and not 1e-9: the oracle itself moves by 5e-9 when only the summation
+order of its dot products changes (tests/test_oracle_kat.py::
+test_pcg_rounding_noise_floor), so a tighter bound would test rounding order,
+not the algorithm.  The mixed FP32/FP64 refinement form must stay within
+1e-6 of the FP64 result.  Integer outputs (node numbering, dof maps) must be
+identical.
 """
 import json
 import os
@@ -17,7 +21,7 @@ from specfem3d_geotech_gb300 import meshgen
 
 pytestmark = pytest.mark.gpu
 
-FP64_TOL = 1e-9
+FP64_TOL = 1e-8
 MIXED_TOL = 1e-6
 
 

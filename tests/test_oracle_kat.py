@@ -177,3 +177,28 @@ def test_golden_sweep_bracket():
     # plastic iterations grow towards failure
     nl = [r["nl_iter"] for r in rows[:-1]]
     assert nl == sorted(nl)
+
+
+def test_pcg_rounding_noise_floor():
+    """Summation order alone moves a cg_tol = 1e-8 PCG solve by ~5e-9 (relative L2).
+
+    This bounds how closely any reimplementation can match the reference in
+    FP64: the GPU parity tests use 1e-8, not a tighter figure.
+    """
+    om = OracleModel(meshgen.slope2d())
+    km, dp, ext = om.stiffness_bodyload()
+    dinv = np.where(np.arange(om.neq + 1) > 0, 1.0 / np.where(dp == 0, 1, dp), 0.0)
+    ge = om.arrays()["gdof_elmt"]
+    sol = []
+    try:
+        for order in (0, 1):
+            L.orc_set_dot_order(order)
+            u = np.zeros(om.neq + 1)
+            err, it = pyoracle.pcg_solver(om.neq, om.nelmt, km, u, ext, dinv, ge, 5000, 1e-8)
+            assert err == 0
+            sol.append((u, it))
+    finally:
+        L.orc_set_dot_order(0)
+    d = np.linalg.norm(sol[0][0] - sol[1][0]) / np.linalg.norm(sol[0][0])
+    assert 1e-10 < d < 1e-8
+    assert abs(sol[0][1] - sol[1][1]) <= 2
