@@ -135,6 +135,20 @@ typedef struct sg_trial_result {
 int sg_srf_trials(sg_model* model, const sg_control* ctl, int k, const double* srf,
                   sg_trial_result* results, double* x_out);
 
+/* ---- continuous batching of SRF trials on one model -------------------
+ * A batch has kmax (<= 16) slots.  sg_batch_add starts a trial in a free
+ * slot at any time, sg_batch_step advances every running trial by up to
+ * nsteps plastic iterations (one shared multi-RHS solve per iteration),
+ * sg_batch_poll reports a slot (state 0 free, 1 running, 2 finished) and
+ * sg_batch_release frees a finished slot for the next trial.  sg_srf_trials
+ * is begin + add + step-to-completion + end. */
+int sg_batch_begin(sg_model* model, const sg_control* ctl, int kmax);
+int sg_batch_add(sg_model* model, double srf, int* slot);
+int sg_batch_step(sg_model* model, int nsteps, int* nlive);
+int sg_batch_poll(sg_model* model, int slot, sg_trial_result* result, int* state);
+int sg_batch_release(sg_model* model, int slot);
+int sg_batch_end(sg_model* model);
+
 /* Stress state of the last trial batch: stress[(t*nelmt + e)*27*6 + i*6 + s] for trial t. */
 int sg_last_stress(sg_model* model, int trial, double* stress_elmt);
 
@@ -167,6 +181,10 @@ int sg_excavation(sg_model* model, const sg_control* ctl, int s0_type, double z0
  * Collected with CUDA events on the context's stream when enabled. */
 int sg_profile_enable(sg_ctx* ctx, int on);
 int sg_profile_read(sg_ctx* ctx, double* ms, long long* counts);
+/* CUDA-event marks on the context's stream (id 0..15) and the device time
+ * between two marks in milliseconds (synchronises on mark b). */
+int sg_timer_mark(sg_ctx* ctx, int id);
+double sg_timer_ms(sg_ctx* ctx, int a, int b);
 
 #ifdef __cplusplus
 }

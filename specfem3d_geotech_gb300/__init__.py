@@ -35,7 +35,8 @@ EXPORTED = (
     "sg_create", "sg_create_status", "sg_destroy", "sg_last_error", "sg_hbm_used", "sg_pcg_solve",
     "sg_model_from_hex8", "sg_model_from_deck", "sg_model_free", "sg_model_info", "sg_model_arrays",
     "sg_model_control", "sg_model_stiffness", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
-    "sg_excavation", "sg_profile_enable", "sg_profile_read",
+    "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
+    "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms",
 )
 
 
@@ -115,6 +116,22 @@ def lib(path: Optional[str] = None):
     L.sg_profile_enable.argtypes = [vp, i]
     L.sg_profile_read.restype = i
     L.sg_profile_read.argtypes = [vp, vp, vp]
+    L.sg_batch_begin.restype = i
+    L.sg_batch_begin.argtypes = [vp, C.POINTER(Control), i]
+    L.sg_batch_add.restype = i
+    L.sg_batch_add.argtypes = [vp, d, C.POINTER(C.c_int)]
+    L.sg_batch_step.restype = i
+    L.sg_batch_step.argtypes = [vp, i, C.POINTER(C.c_int)]
+    L.sg_batch_poll.restype = i
+    L.sg_batch_poll.argtypes = [vp, i, C.POINTER(TrialResult), C.POINTER(C.c_int)]
+    L.sg_batch_release.restype = i
+    L.sg_batch_release.argtypes = [vp, i]
+    L.sg_batch_end.restype = i
+    L.sg_batch_end.argtypes = [vp]
+    L.sg_timer_mark.restype = i
+    L.sg_timer_mark.argtypes = [vp, i]
+    L.sg_timer_ms.restype = d
+    L.sg_timer_ms.argtypes = [vp, i, i]
     _lib = L
     return L
 
@@ -146,6 +163,13 @@ class Context:
     @property
     def hbm_used(self) -> int:
         return int(lib().sg_hbm_used(self.h))
+
+    def mark(self, i: int):
+        """Record CUDA event `i` on the context's stream."""
+        lib().sg_timer_mark(self.h, i)
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        return float(lib().sg_timer_ms(self.h, a, b))
 
     def profile(self, on: bool = True):
         lib().sg_profile_enable(self.h, 1 if on else 0)
@@ -302,6 +326,43 @@ class Model:
         if st:
             raise SgError(st, self.ctx.last_error)
         return v.value, nt.value, nr.value
+
+    # ---- continuous batching -------------------------------------------
+    def batch_begin(self, ctl: Control, kmax: int):
+        self._batch_ctl = ctl
+        st = lib().sg_batch_begin(self.h, C.byref(ctl), kmax)
+        if st:
+            raise SgError(st, self.ctx.last_error)
+
+    def batch_add(self, srf: float) -> int:
+        slot = C.c_int(-1)
+        st = lib().sg_batch_add(self.h, srf, C.byref(slot))
+        if st:
+            raise SgError(st, self.ctx.last_error)
+        return slot.value
+
+    def batch_step(self, nsteps: int = 1) -> int:
+        n = C.c_int(0)
+        st = lib().sg_batch_step(self.h, nsteps, C.byref(n))
+        if st not in (SG_OK, SG_ERR_NOCONV):
+            raise SgError(st, self.ctx.last_error)
+        return n.value
+
+    def batch_poll(self, slot: int):
+        r = TrialResult()
+        state = C.c_int(0)
+        st = lib().sg_batch_poll(self.h, slot, C.byref(r), C.byref(state))
+        if st:
+            raise SgError(st, "sg_batch_poll")
+        return state.value, r.as_dict()
+
+    def batch_release(self, slot: int):
+        st = lib().sg_batch_release(self.h, slot)
+        if st:
+            raise SgError(st, "sg_batch_release")
+
+    def batch_end(self):
+        lib().sg_batch_end(self.h)
 
     def excavation(self, ctl: Control, s0_type: int, z0: float, s0: float, k0: float, excavid: Sequence[int],
                    nexcavid: Optional[Sequence[int]] = None, ninc: int = 1, srf: float = 1.0):

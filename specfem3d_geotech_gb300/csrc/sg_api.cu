@@ -8,6 +8,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -52,6 +53,8 @@ struct sg_ctx {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
   std::vector<std::pair<int, int>> ev_used;  // (pool index, category)
   double* pin = nullptr;                     // pinned scratch for scalars
+  cudaEvent_t marks[16] = {};
+  long long launch0 = 0;
   int* d_nbr = nullptr;
   int* d_entry = nullptr;
   // drop-in cache: the reference calls pcg_solver with the same dof map every
@@ -263,6 +266,9 @@ sg_ctx* sg_create(int device, size_t hbm_budget) {
   }
   cudaMallocHost((void**)&c->pin, 4096);
   upload_constants();
+  // SG_APPLY_VARIANT=0 selects the register-staged element apply instead of
+  // the TMA pipeline (kept for cross-checking the two).
+  if (const char* v = std::getenv("SG_APPLY_VARIANT")) set_apply_variant(std::atoi(v));
   const KsTables& T = ks_tables();
   c->d_nbr = c->alloc<int>(NGLL * KS_NBR);
   c->d_entry = c->alloc<int>(KS_NNZ);
@@ -303,6 +309,7 @@ void sg_destroy(sg_ctx* c) {
   for (auto& kv : c->live) cudaFree(kv.first);
   c->live.clear();
   for (auto& e : c->ev_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
+  for (auto& e : c->marks) if (e) cudaEventDestroy(e);
   if (c->pin) cudaFreeHost(c->pin);
   cudaStreamDestroy(c->stream);
   delete c;
@@ -316,7 +323,22 @@ int sg_profile_enable(sg_ctx* c, int on) {
   c->prof_flush();
   c->prof = Profile();
   c->prof.on = on != 0;
+  c->launch0 = launch_count();
   return SG_OK;
+}
+
+int sg_timer_mark(sg_ctx* c, int id) {
+  if (!c || id < 0 || id >= 16) return SG_ERR_BADARG;
+  if (!c->marks[id]) cudaEventCreate(&c->marks[id]);
+  return c->check(cudaEventRecord(c->marks[id], c->stream), "timer mark") ? SG_OK : SG_ERR_CUDA;
+}
+
+double sg_timer_ms(sg_ctx* c, int a, int b) {
+  if (!c || a < 0 || b < 0 || a >= 16 || b >= 16 || !c->marks[a] || !c->marks[b]) return -1.0;
+  cudaEventSynchronize(c->marks[b]);
+  float ms = -1.f;
+  if (cudaEventElapsedTime(&ms, c->marks[a], c->marks[b]) != cudaSuccess) return -1.0;
+  return ms;
 }
 
 int sg_profile_read(sg_ctx* c, double* ms, long long* counts) {
@@ -324,6 +346,7 @@ int sg_profile_read(sg_ctx* c, double* ms, long long* counts) {
   c->prof_flush();
   for (int i = 0; i < 8; ++i) ms[i] = c->prof.ms[i];
   for (int i = 0; i < 4; ++i) counts[i] = c->prof.counts[i];
+  counts[1] = launch_count() - c->launch0;
   return SG_OK;
 }
 
@@ -430,8 +453,26 @@ struct TrialWork {
   double* red = nullptr;
 };
 
+struct Slot {
+  int used = 0;   // holds a trial (running or finished, not yet released)
+  int live = 0;   // still iterating
+  double dt = 0;  // pseudo-time step of the trial (dt_viscoplas)
+  sg_trial_result res{};
+  std::chrono::steady_clock::time_point t0;
+};
+
+struct Batch {
+  bool open = false;
+  sg_control ctl{};
+  int kmax = 0, KR = 0;
+  Slot slot[16];
+  double* d_nuf = nullptr;
+  bool restiff = false;
+};
+
 struct sg_model {
   sg_ctx* ctx = nullptr;
+  Batch B;
   HostMesh H;
   int precision = SG_PREC_FP64;
   double* d_coord = nullptr;
@@ -829,146 +870,222 @@ static int linear_solve(sg_model* M, const sg_control* ctl, const Op& op64, cons
 }
 
 // ---------------------------------------------------------------------------
-// k concurrent SRF trials of slope3d (src/slope.F90:244-443)
+// Trial batch engine: up to 16 slots, each an independent SRF trial of
+// slope3d (src/slope.F90:244-443) on the model's mesh.  All live slots share
+// one batched linear solve per plastic iteration (the slots are the columns
+// of the multi-RHS element apply); each keeps its own factored properties,
+// pseudo-time step, plastic strain, stress, body load and counters.  A slot
+// freed by a finished trial can take a new trial while the others run
+// (continuous batching).
 // ---------------------------------------------------------------------------
-static int run_trials(sg_model* M, const sg_control* ctl, int k, const double* srf, sg_trial_result* res,
-                      double* x_out) {
+static int batch_end_impl(sg_model* M);
+
+static int batch_begin_impl(sg_model* M, const sg_control* ctl, int kmax) {
   sg_ctx* c = M->ctx;
   HostMesh& h = M->H;
-  if (k < 1 || k > 16 || !ctl || !srf || !res) return SG_ERR_BADARG;
+  if (!ctl || kmax < 1 || kmax > 16) return SG_ERR_BADARG;
+  if (ctl->precision != M->precision) {
+    c->err = "control precision differs from the model's precision";
+    return SG_ERR_BADARG;
+  }
+  if (M->B.open) batch_end_impl(M);
   cudaSetDevice(c->device);
-  cudaStream_t s = c->stream;
-  const int n1 = h.neq + 1, KR = next_pow2(k), ne = h.nelmt;
-  const auto t_start = std::chrono::steady_clock::now();
+  const int n1 = h.neq + 1, KR = next_pow2(kmax), ne = h.nelmt;
   if (!model_work(M, KR, n1, ne)) { c->err = "trial workspace does not fit the HBM budget"; return SG_ERR_OOM; }
+  Batch& B = M->B;
+  B = Batch();
+  B.open = true;
+  B.ctl = *ctl;
+  B.kmax = kmax;
+  B.KR = KR;
+  cudaStream_t s = c->stream;
   TrialWork& W = M->W;
-  // per-trial factored properties
-  std::vector<double> dt(k);
-  std::vector<MatF> mf_all((size_t)KR * h.nmatblk);
-  bool restiff = false;
-  std::vector<double> nuf_first;
-  for (int t = 0; t < k; ++t) {
-    std::vector<double> cohf, nuf, phif, psif;
-    int istat = strength_reduction(h, srf[t], ctl->phinu != 0, cohf, nuf, phif, psif);
-    if (istat == 1) {
-      if (k > 1) { c->err = "phi-nu correction changes the stiffness: run such trials one at a time"; return SG_ERR_BADARG; }
-      restiff = true;
-      nuf_first = nuf;
-    }
-    dt[t] = dt_viscoplas(nuf, phif, h.ym, nullptr);
-    std::vector<MatF> mf;
-    make_matf(h, h.ym, nuf, phif, cohf, psif, mf);
-    std::copy(mf.begin(), mf.end(), mf_all.begin() + (size_t)t * h.nmatblk);
-  }
-  cudaMemcpyAsync(W.mf, mf_all.data(), sizeof(MatF) * mf_all.size(), cudaMemcpyHostToDevice, s);
-  double* d_nuf = nullptr;
-  if (restiff) {
-    d_nuf = c->alloc<double>(h.nmatblk);
-    cudaMemcpyAsync(d_nuf, nuf_first.data(), sizeof(double) * h.nmatblk, cudaMemcpyHostToDevice, s);
-    model_stiffness(M, nullptr, ne, d_nuf, M->T, M->d_ge, n1, false);
-  }
-  const size_t nv = (size_t)n1 * KR;
-  const size_t nst = (size_t)ne * NGLL * NST;
+  const size_t nv = (size_t)n1 * KR, nst = (size_t)ne * NGLL * NST;
   cudaMemsetAsync(W.x, 0, sizeof(double) * nv, s);
   cudaMemsetAsync(W.oldx, 0, sizeof(double) * nv, s);
   cudaMemsetAsync(W.bodyload, 0, sizeof(double) * nv, s);
   cudaMemsetAsync(W.evpt, 0, sizeof(double) * nst * KR, s);
   cudaMemsetAsync(W.stress, 0, sizeof(double) * nst * KR, s);
+  return c->check(cudaGetLastError(), "batch begin") ? SG_OK : SG_ERR_CUDA;
+}
+
+static int batch_add_impl(sg_model* M, double srf, int* slot_out) {
+  sg_ctx* c = M->ctx;
+  HostMesh& h = M->H;
+  Batch& B = M->B;
+  if (!B.open || srf <= 0.0) return SG_ERR_BADARG;
+  int j = -1;
+  for (int t = 0; t < B.kmax; ++t)
+    if (!B.slot[t].used) { j = t; break; }
+  if (j < 0) { c->err = "no free trial slot"; return SG_ERR_BADARG; }
+  std::vector<double> cohf, nuf, phif, psif;
+  int istat = strength_reduction(h, srf, B.ctl.phinu != 0, cohf, nuf, phif, psif);
+  cudaStream_t s = c->stream;
+  TrialWork& W = M->W;
+  if (istat == 1) {
+    // stiffness_bodyload is redone with the corrected Poisson ratios
+    // (src/slope.F90:259-270); the batch then holds this one trial only.
+    bool other = false;
+    for (int t = 0; t < B.kmax; ++t) other = other || B.slot[t].used;
+    if (other || B.kmax > 1) {
+      c->err = "phi-nu correction changes the stiffness: run such trials one at a time";
+      return SG_ERR_BADARG;
+    }
+    if (!B.d_nuf) B.d_nuf = c->alloc<double>(h.nmatblk);
+    cudaMemcpyAsync(B.d_nuf, nuf.data(), sizeof(double) * h.nmatblk, cudaMemcpyHostToDevice, s);
+    model_stiffness(M, nullptr, h.nelmt, B.d_nuf, M->T, M->d_ge, h.neq + 1, false);
+    B.restiff = true;
+  }
+  std::vector<MatF> mf;
+  make_matf(h, h.ym, nuf, phif, cohf, psif, mf);
+  cudaMemcpyAsync(W.mf + (size_t)j * h.nmatblk, mf.data(), sizeof(MatF) * h.nmatblk, cudaMemcpyHostToDevice, s);
+  const int n1 = h.neq + 1;
+  const size_t nst = (size_t)h.nelmt * NGLL * NST;
+  launch_col_zero(n1, B.KR, j, W.x, W.oldx, W.bodyload, s);
+  cudaMemsetAsync(W.evpt + nst * j, 0, sizeof(double) * nst, s);
+  cudaMemsetAsync(W.stress + nst * j, 0, sizeof(double) * nst, s);
+  Slot& S = B.slot[j];
+  S = Slot();
+  S.used = 1;
+  S.live = 1;
+  S.dt = dt_viscoplas(nuf, phif, h.ym, nullptr);
+  S.res.srf = srf;
+  S.t0 = std::chrono::steady_clock::now();
+  if (slot_out) *slot_out = j;
+  return c->check(cudaGetLastError(), "batch add") ? SG_OK : SG_ERR_CUDA;
+}
+
+// Nodal displacement maxima of a finished slot (src/slope.F90:400-415).
+static void slot_finish(sg_model* M, int j) {
+  sg_ctx* c = M->ctx;
+  Slot& S = M->B.slot[j];
+  double red[64];
+  launch_disp_max(M->H.nnode, M->d_gdof, M->W.x, M->B.KR, j, M->W.b64.part, c->stream);
+  reduce_read(c, M->W.b64.part, NPART, 1, 2, 3, M->W.red, red);
+  S.res.uxmax = red[0];
+  S.res.umax = red[1];
+  S.res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - S.t0).count();
+  S.live = 0;
+}
+
+// One plastic iteration (src/slope.F90:285-391) of every live slot.
+static int batch_iteration(sg_model* M) {
+  sg_ctx* c = M->ctx;
+  HostMesh& h = M->H;
+  Batch& B = M->B;
+  TrialWork& W = M->W;
+  const sg_control* ctl = &B.ctl;
+  cudaStream_t s = c->stream;
+  const int n1 = h.neq + 1, KR = B.KR, ne = h.nelmt, k = B.kmax;
+  const size_t nst = (size_t)ne * NGLL * NST;
+  std::vector<int> live(k, 0);
+  bool any = false;
+  for (int t = 0; t < k; ++t) { live[t] = B.slot[t].live; any = any || live[t]; }
+  if (!any) return SG_OK;
   Op op64, op32;
   op64.K = M->d_K64; op64.ge = M->d_ge; op64.nelmt = ne; op64.T = &M->T;
   op32 = op64;
   op32.K = M->d_K32;
-  std::vector<int> live(k, 1);
-  std::vector<int> done(k, 0);
+  launch_load_combine(n1, KR, M->d_extload, W.bodyload, W.load, s);
+  SolveStats St;
+  int st = linear_solve(M, ctl, op64, op32, k, live, St, M->d_dprecon, M->d_dprecon32);
   for (int t = 0; t < k; ++t) {
-    res[t] = sg_trial_result();
-    res[t].srf = srf[t];
-  }
-  int status = SG_OK;
-  double red[64];
-  for (int nl_iter = 1; nl_iter <= ctl->nl_maxiter; ++nl_iter) {
-    bool any = false;
-    for (int t = 0; t < k; ++t) any = any || live[t];
-    if (!any) break;
-    launch_load_combine(n1, KR, M->d_extload, W.bodyload, W.load, s);
-    SolveStats S;
-    int st = linear_solve(M, ctl, op64, op32, k, live, S, M->d_dprecon, M->d_dprecon32);
+    if (!live[t]) continue;
+    Slot& S = B.slot[t];
+    S.res.nl_iter += 1;
     if (st != SG_OK) {
       // the reference stops the program on a PCG failure (error_stop, src/slope.F90:294)
-      for (int t = 0; t < k; ++t)
-        if (live[t]) { res[t].errcode = st; res[t].nl_iter = nl_iter; live[t] = 0; }
-      status = st;
-      break;
+      S.res.errcode = st;
+      slot_finish(M, t);
+      continue;
     }
-    for (int t = 0; t < k; ++t)
-      if (live[t]) { res[t].cg_tot += S.iters[t]; res[t].refine_steps += S.refine; }
-    if (ctl->allelastic) {
-      for (int t = 0; t < k; ++t) {
-        if (!live[t]) continue;
-        launch_elastic_stress(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, W.x + 0, W.mf + (size_t)t * h.nmatblk, 0,
-                              W.stress + nst * t, s);
-        res[t].nl_iter = nl_iter; res[t].converged = 0; res[t].failed = (nl_iter == ctl->nl_maxiter);
-        live[t] = 0;
-      }
-      break;
-    }
-    // uerr = max|x-oldx| / max|x|; oldx = x (src/slope.F90:307-309)
-    launch_nl_check(n1, KR, k, W.x, W.oldx, W.b64.part, s);
-    reduce_read(c, W.b64.part, NPART, KR, 2, 3, W.red, red);
-    int mask[16] = {0};
-    std::vector<int> fin(k, 0), conv(k, 0);
+    S.res.cg_tot += St.iters[t];
+    S.res.refine_steps += St.refine;
+  }
+  if (st != SG_OK) return st;
+  if (ctl->allelastic) {
     for (int t = 0; t < k; ++t) {
       if (!live[t]) continue;
-      double uerr = red[2 * t] / red[2 * t + 1];
-      res[t].uerr = uerr;
-      conv[t] = uerr <= ctl->nl_tol;
-      fin[t] = conv[t] || nl_iter == ctl->nl_maxiter;
-      mask[t] = 1;
-      int ev = c->prof_begin();
-      launch_stress_update(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, W.x, KR, t, W.mf + (size_t)t * h.nmatblk,
-                           dt[t], conv[t], fin[t], W.evpt + nst * t, W.stress + nst * t, W.Yb, KR, t,
-                           M->d_fpart + NPART * (t & 1), s);
-      c->prof_end(ev, 4);
-      reduce_read(c, M->d_fpart + NPART * (t & 1), NPART, 1, 1, 1, W.red, red + 32);
-      res[t].fmax = red[32];
+      launch_elastic_stress(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, W.x, KR, t, W.mf + (size_t)t * h.nmatblk, 0,
+                            W.stress + nst * t, s);
+      Slot& S = B.slot[t];
+      S.res.failed = (S.res.nl_iter == ctl->nl_maxiter);
+      slot_finish(M, t);
     }
-    // bodyload(egdof) += bload for the trials that continue
-    int gmask[16] = {0};
-    bool anyg = false;
-    for (int t = 0; t < k; ++t) { gmask[t] = mask[t] && !fin[t]; anyg = anyg || gmask[t]; }
-    if (anyg) {
-      cudaMemcpyAsync(W.colmask, gmask, sizeof(int) * 16, cudaMemcpyHostToDevice, s);
-      launch_gather_plain<double>(M->T, KR, W.Yb, W.bodyload, 1, W.colmask, s);
-    }
-    for (int t = 0; t < k; ++t) {
-      if (!live[t] || !fin[t]) continue;
-      res[t].nl_iter = nl_iter;
-      res[t].converged = conv[t];
-      res[t].failed = (nl_iter == ctl->nl_maxiter);
-      live[t] = 0;
-    }
+    return SG_OK;
   }
-  // summary maxima (src/slope.F90:400-415)
+  // uerr = max|x-oldx| / max|x|; oldx = x (src/slope.F90:307-309)
+  double red[64];
+  launch_nl_check(n1, KR, k, W.x, W.oldx, W.b64.part, s);
+  reduce_read(c, W.b64.part, NPART, KR, 2, 3, W.red, red);
+  std::vector<int> fin(k, 0), conv(k, 0);
+  int gmask[16] = {0};
+  bool anyg = false;
   for (int t = 0; t < k; ++t) {
-    launch_disp_max(h.nnode, M->d_gdof, W.x, KR, t, W.b64.part, s);
-    reduce_read(c, W.b64.part, NPART, 1, 2, 3, W.red, red);
-    res[t].uxmax = red[0];
-    res[t].umax = red[1];
+    if (!live[t]) continue;
+    Slot& S = B.slot[t];
+    double uerr = red[2 * t] / red[2 * t + 1];
+    S.res.uerr = uerr;
+    conv[t] = uerr <= ctl->nl_tol;
+    fin[t] = conv[t] || S.res.nl_iter == ctl->nl_maxiter;
+    int ev = c->prof_begin();
+    launch_stress_update(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, W.x, KR, t, W.mf + (size_t)t * h.nmatblk, S.dt,
+                         conv[t], fin[t], W.evpt + nst * t, W.stress + nst * t, W.Yb, KR, t, M->d_fpart, s);
+    c->prof_end(ev, 4);
+    reduce_read(c, M->d_fpart, NPART, 1, 1, 1, W.red, red + 32);
+    S.res.fmax = red[32];
+    gmask[t] = !fin[t];
+    anyg = anyg || gmask[t];
   }
+  // bodyload(egdof) += bload for the slots that continue
+  if (anyg) {
+    cudaMemcpyAsync(W.colmask, gmask, sizeof(int) * 16, cudaMemcpyHostToDevice, s);
+    launch_gather_plain<double>(M->T, KR, W.Yb, W.bodyload, 1, W.colmask, s);
+  }
+  for (int t = 0; t < k; ++t) {
+    if (!live[t] || !fin[t]) continue;
+    Slot& S = B.slot[t];
+    S.res.converged = conv[t];
+    S.res.failed = (S.res.nl_iter == ctl->nl_maxiter);
+    slot_finish(M, t);
+  }
+  if (apply_error_flag(s)) { c->err = "element apply: bulk-copy wait timed out"; return SG_ERR_TIMEOUT; }
+  return c->check(cudaGetLastError(), "plastic iteration") ? SG_OK : SG_ERR_CUDA;
+}
+
+static int batch_end_impl(sg_model* M) {
+  Batch& B = M->B;
+  if (!B.open) return SG_OK;
+  if (B.restiff) model_stiffness(M, nullptr, M->H.nelmt, M->d_nu, M->T, M->d_ge, M->H.neq + 1, false);
+  M->ctx->release(B.d_nuf);
+  B = Batch();
+  return SG_OK;
+}
+
+static int run_trials(sg_model* M, const sg_control* ctl, int k, const double* srf, sg_trial_result* res,
+                      double* x_out) {
+  if (k < 1 || k > 16 || !ctl || !srf || !res) return SG_ERR_BADARG;
+  int st = batch_begin_impl(M, ctl, k);
+  if (st != SG_OK) return st;
+  for (int t = 0; t < k && st == SG_OK; ++t) st = batch_add_impl(M, srf[t], nullptr);
+  while (st == SG_OK) {
+    bool any = false;
+    for (int t = 0; t < k; ++t) any = any || M->B.slot[t].live;
+    if (!any) break;
+    st = batch_iteration(M);
+  }
+  for (int t = 0; t < k; ++t) res[t] = M->B.slot[t].res;
   if (x_out) {
-    std::vector<double> hx(nv);
-    cudaMemcpy(hx.data(), W.x, sizeof(double) * nv, cudaMemcpyDeviceToHost);
+    const int n1 = M->H.neq + 1, KR = M->B.KR;
+    std::vector<double> hx((size_t)n1 * KR);
+    cudaMemcpyAsync(hx.data(), M->W.x, sizeof(double) * hx.size(), cudaMemcpyDeviceToHost, M->ctx->stream);
+    cudaStreamSynchronize(M->ctx->stream);
     for (int t = 0; t < k; ++t)
       for (int i = 0; i < n1; ++i) x_out[(size_t)t * n1 + i] = hx[(size_t)i * KR + t];
   }
-  if (restiff) {
-    model_stiffness(M, nullptr, ne, M->d_nu, M->T, M->d_ge, n1, false);
-    c->release(d_nuf);
-  }
-  if (!c->check(cudaStreamSynchronize(s), "trials")) status = SG_ERR_CUDA;
-  double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-  for (int t = 0; t < k; ++t) res[t].seconds = secs;
-  return status;
+  batch_end_impl(M);
+  if (!M->ctx->check(cudaStreamSynchronize(M->ctx->stream), "trials") && st == SG_OK) st = SG_ERR_CUDA;
+  return st;
 }
 
 extern "C" {
@@ -978,6 +1095,41 @@ int sg_srf_trials(sg_model* M, const sg_control* ctl, int k, const double* srf, 
   if (!M) return SG_ERR_BADARG;
   return run_trials(M, ctl, k, srf, results, x_out);
 }
+
+int sg_batch_begin(sg_model* M, const sg_control* ctl, int kmax) {
+  return M ? batch_begin_impl(M, ctl, kmax) : SG_ERR_BADARG;
+}
+int sg_batch_add(sg_model* M, double srf, int* slot) { return M ? batch_add_impl(M, srf, slot) : SG_ERR_BADARG; }
+int sg_batch_step(sg_model* M, int nsteps, int* nlive) {
+  if (!M || !M->B.open || nsteps < 0) return SG_ERR_BADARG;
+  int st = SG_OK;
+  for (int i = 0; i < nsteps && st == SG_OK; ++i) {
+    bool any = false;
+    for (int t = 0; t < M->B.kmax; ++t) any = any || M->B.slot[t].live;
+    if (!any) break;
+    st = batch_iteration(M);
+  }
+  if (nlive) {
+    int n = 0;
+    for (int t = 0; t < M->B.kmax; ++t) n += M->B.slot[t].live;
+    *nlive = n;
+  }
+  return st;
+}
+int sg_batch_poll(sg_model* M, int slot, sg_trial_result* res, int* state) {
+  if (!M || !M->B.open || slot < 0 || slot >= M->B.kmax) return SG_ERR_BADARG;
+  const Slot& S = M->B.slot[slot];
+  if (res) *res = S.res;
+  if (state) *state = !S.used ? 0 : (S.live ? 1 : 2);
+  return SG_OK;
+}
+int sg_batch_release(sg_model* M, int slot) {
+  if (!M || !M->B.open || slot < 0 || slot >= M->B.kmax) return SG_ERR_BADARG;
+  if (M->B.slot[slot].live) return SG_ERR_BADARG;
+  M->B.slot[slot] = Slot();
+  return SG_OK;
+}
+int sg_batch_end(sg_model* M) { return M ? batch_end_impl(M) : SG_ERR_BADARG; }
 
 int sg_last_stress(sg_model* M, int trial, double* stress_elmt) {
   if (!M || !stress_elmt || trial < 0 || trial >= M->W.KR) return SG_ERR_BADARG;
@@ -1078,7 +1230,7 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
       std::vector<int> act(1, 1);
       status = linear_solve(M, &c0, op64, op32, 1, act, S, M->d_dprecon, M->d_dprecon32);
       if (status != SG_OK) goto done;
-      launch_elastic_stress(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, M->W.x, d_mf, 0, stress, s);
+      launch_elastic_stress(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, M->W.x, 1, 0, d_mf, 0, stress, s);
     }
   } else {
     status = SG_ERR_BADARG;

@@ -16,11 +16,19 @@
 // All reductions use a fixed grid (NPART blocks) and fixed-order trees, so a
 // run is bitwise reproducible on the same device type.
 #include <cstdio>
+#include <algorithm>
 #include <type_traits>
 
 #include "sg_kernels.cuh"
 
+#include <atomic>
+
 namespace sg {
+
+// host-side count of kernel launches issued by this library
+std::atomic<long long> g_launch_count{0};
+long long launch_count() { return g_launch_count.load(); }
+#define SG_LAUNCH ++g_launch_count,
 
 // D[p][m] = derivative of the m-th 1D Lagrange polynomial on the GLL points
 // {-1, 0, 1} evaluated at point p (lagrange1dGLL, src/gll_library.f90:257-299);
@@ -151,7 +159,7 @@ __global__ void k_geometry(const double* __restrict__ g_coord, const int* __rest
 
 void launch_geometry(const double* g_coord, const int* g_num, int nelmt, double* geo, cudaStream_t s) {
   int n = nelmt * NGLL;
-  k_geometry<<<(n + 127) / 128, 128, 0, s>>>(g_coord, g_num, nelmt, geo);
+  SG_LAUNCH k_geometry<<<(n + 127) / 128, 128, 0, s>>>(g_coord, g_num, nelmt, geo);
 }
 
 // deriv(:,n) at GLL point i: sum_a Jinv(:,a) dlagrange(a,i,n).  dlagrange is
@@ -260,7 +268,7 @@ void launch_stiffness(const double* geo, const int* mat_id, const int* elist, in
                       const double* nu, const double* gam, double* Ks64, float* Ks32, double* Ydiag,
                       double* Ygrav, const int* d_entry, cudaStream_t s) {
   if (nel <= 0) return;
-  k_stiffness<<<nel, STIFF_THREADS, 0, s>>>(geo, mat_id, elist, nel, ym, nu, gam, Ks64, Ks32, Ydiag, Ygrav,
+  SG_LAUNCH k_stiffness<<<nel, STIFF_THREADS, 0, s>>>(geo, mat_id, elist, nel, ym, nu, gam, Ks64, Ks32, Ydiag, Ygrav,
                                            d_entry);
 }
 
@@ -282,13 +290,16 @@ __global__ void k_expand_dense(const double* __restrict__ Ks, int nel, double* _
 }
 
 void launch_expand_dense(const double* Ks64, int nel, double* dense, const int* d_entry, cudaStream_t s) {
-  if (nel > 0) k_expand_dense<<<nel, 256, 0, s>>>(Ks64, nel, dense, d_entry);
+  if (nel > 0) SG_LAUNCH k_expand_dense<<<nel, 256, 0, s>>>(Ks64, nel, dense, d_entry);
 }
 
 // ---------------------------------------------------------------------------
 // Element apply.
 // ---------------------------------------------------------------------------
 constexpr int APPLY_WARPS = 4;
+// 0 = register-staged loads, 1 = TMA bulk-copy pipeline (default)
+int g_apply_variant = 1;
+void set_apply_variant(int v) { g_apply_variant = v; }
 
 // Dense FP64 81x81, one right-hand side (the drop-in).  One warp per element,
 // lane l owns rows l, l+32, l+64; column c of K_e is 81 contiguous doubles,
@@ -340,7 +351,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse(
     const V* __restrict__ z, int combine, V* __restrict__ Y, const ColState* __restrict__ cs,
     const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g) {
   if (G && G->all_done) return;
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   int* nbr = (int*)smem;                                   // 27*19 ints (2064 B incl. pad)
   V* wbase = (V*)(smem + 2064);
   constexpr int WSTRIDE = KS_STRIDE + ((NEDOF * KR + 3) & ~3);  // keeps every warp region 16-byte aligned
@@ -405,6 +416,151 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse(
   }
 }
 
+// ---- TMA-staged variant: 1D bulk copies (cp.async.bulk) of each element's
+// matrix into a two-stage per-warp ring, completion tracked by mbarriers.
+// Lane 0 issues the copy of the warp's next element before the warp computes
+// the current one, so the HBM stream overlaps the shared-memory matvec.
+// Every wait is bounded: on timeout the kernel records the fault in *err and
+// the warp stops after draining its own copies (also bounded).
+__device__ int g_apply_err;  // set to 1 by a timed-out mbarrier wait
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// returns false if the phase did not complete within the bound
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  for (int tries = 0; tries < (1 << 22); ++tries) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+template <typename V, int KR>
+__global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
+    const V* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const V* __restrict__ pold,
+    const V* __restrict__ z, int combine, V* __restrict__ Y, const ColState* __restrict__ cs,
+    const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g) {
+  if (G && G->all_done) return;
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int PST = (NEDOF * KR + 3) & ~3;
+  constexpr int WSTRIDE = 2 * KS_STRIDE + PST;     // two K stages + the p tile
+  constexpr unsigned KBYTES = KS_STRIDE * sizeof(V);
+  int* nbr = (int*)smem;                           // 27*19 ints
+  uint64_t* bars = (uint64_t*)(smem + 2064);       // 2 mbarriers per warp
+  V* wbase = (V*)(smem + 2064 + 16 * APPLY_WARPS + 48);  // 128-byte aligned base (2064+64+48 = 2176)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  V* kbuf0 = wbase + (size_t)warp * WSTRIDE;
+  V* kbuf1 = kbuf0 + KS_STRIDE;
+  V* ps = kbuf1 + KS_STRIDE;
+  uint64_t* bar = bars + 2 * warp;
+  for (int t = threadIdx.x; t < NGLL * KS_NBR; t += blockDim.x) nbr[t] = nbr_g[t];
+  if (lane == 0) {
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  double beta[KR];
+#pragma unroll
+  for (int j = 0; j < KR; ++j) beta[j] = combine ? cs[j].beta : 0.0;
+  __syncthreads();
+  const int stride = gridDim.x * APPLY_WARPS;
+  int e = blockIdx.x * APPLY_WARPS + warp;
+  if (e < nelmt && lane == 0) bulk_load(kbuf0, Ks + (size_t)e * KS_STRIDE, KBYTES, bar);
+  int issued = (e < nelmt) ? 1 : 0, waited = 0;
+  for (int i = 0; e < nelmt; ++i, e += stride) {
+    const int en = e + stride;
+    V* kcur = (i & 1) ? kbuf1 : kbuf0;
+    if (en < nelmt && lane == 0) {
+      V* knext = (i & 1) ? kbuf0 : kbuf1;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bulk_load(knext, Ks + (size_t)en * KS_STRIDE, KBYTES, bar + ((i + 1) & 1));
+      ++issued;
+    }
+    if (lane < NGLL) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        int g = ge[(size_t)e * NEDOF + 3 * lane + d];
+#pragma unroll
+        for (int j = 0; j < KR; ++j) {
+          V pv = pold[(size_t)g * KR + j];
+          if (combine) pv = pdir(beta[j], pv, z[(size_t)g * KR + j]);
+          ps[(3 * lane + d) * KR + j] = pv;
+        }
+      }
+    }
+    bool ok = mbar_wait(bar + (i & 1), (unsigned)((i >> 1) & 1));
+    ++waited;
+    if (!ok) {
+      if (lane == 0) atomicExch(&g_apply_err, 1);
+      break;
+    }
+    __syncwarp();
+    if (lane < NGLL) {
+      V acc[3][KR];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int j = 0; j < KR; ++j) acc[c][j] = (V)0;
+      const int* tb = nbr + lane * KS_NBR;
+#pragma unroll 1
+      for (int s = 0; s < KS_NBR; ++s) {
+        int pk = tb[s];
+        int m = pk & 31, kind = (pk >> 5) & 3, off = pk >> 8;
+        int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
+        const V* kb = kcur + off;
+        const V* pm = ps + 3 * m * KR;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            V kv = kb[c * sc + d * sd];
+#pragma unroll
+            for (int j = 0; j < KR; ++j) acc[c][j] = fmav<V>(kv, pm[d * KR + j], acc[c][j]);
+          }
+        }
+      }
+      V* yo = Y + ((size_t)e * NEDOF + 3 * lane) * KR;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int j = 0; j < KR; ++j) yo[c * KR + j] = acc[c][j];
+    }
+    __syncwarp();
+  }
+  // drain copies still in flight after an early stop (bounded)
+  for (int i = waited; i < issued; ++i) mbar_wait(bar + (i & 1), (unsigned)((i >> 1) & 1));
+}
+
+template <typename V, int KR>
+static size_t apply_tma_smem() {
+  return 2176 + (size_t)APPLY_WARPS * (2 * KS_STRIDE + ((NEDOF * KR + 3) & ~3)) * sizeof(V);
+}
+
+int apply_error_flag(cudaStream_t s) {
+  int h = 0;
+  cudaMemcpyFromSymbolAsync(&h, g_apply_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  return h;
+}
+
 template <typename V, int KR>
 static size_t apply_sparse_smem() {
   return 2064 + (size_t)APPLY_WARPS * (KS_STRIDE + ((NEDOF * KR + 3) & ~3)) * sizeof(V);
@@ -417,7 +573,22 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
   int blocks = (nelmt + APPLY_WARPS - 1) / APPLY_WARPS;
   if (dense) {
     if constexpr (std::is_same<V, double>::value && KR == 1)
-      k_apply_dense64<<<blocks, APPLY_WARPS * 32, 0, s>>>((const double*)K, ge, nelmt, p_old, z, combine, Y, cs, G);
+      SG_LAUNCH k_apply_dense64<<<blocks, APPLY_WARPS * 32, 0, s>>>((const double*)K, ge, nelmt, p_old, z, combine, Y, cs, G);
+    return;
+  }
+  if (g_apply_variant == 1) {
+    size_t sm = apply_tma_smem<V, KR>();
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_apply_sparse_tma<V, KR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      attr = true;
+    }
+    // persistent-style grid: each warp walks a strided list of elements
+    int per_sm = (int)(200 * 1024 / sm);
+    if (per_sm < 1) per_sm = 1;
+    int grid = std::min(blocks, 152 * per_sm);
+    SG_LAUNCH k_apply_sparse_tma<V, KR><<<grid, APPLY_WARPS * 32, sm, s>>>((const V*)K, ge, nelmt, p_old, z, combine, Y, cs,
+                                                                 G, d_nbr);
     return;
   }
   size_t sm = apply_sparse_smem<V, KR>();
@@ -426,7 +597,7 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
     cudaFuncSetAttribute(k_apply_sparse<V, KR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     attr = true;
   }
-  k_apply_sparse<V, KR><<<blocks, APPLY_WARPS * 32, sm, s>>>((const V*)K, ge, nelmt, p_old, z, combine, Y, cs, G,
+  SG_LAUNCH k_apply_sparse<V, KR><<<blocks, APPLY_WARPS * 32, sm, s>>>((const V*)K, ge, nelmt, p_old, z, combine, Y, cs, G,
                                                                d_nbr);
 }
 
@@ -499,10 +670,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
     part[(size_t)blockIdx.x * KR + threadIdx.x] = v;
   }
   if (last_block(&G->cntB)) {
+    // all threads: thread t sums blocks t/KR, t/KR + RED_THREADS/KR, ... of column t%KR in order
+    __shared__ double sfin[RED_THREADS];
+    double v = 0.0;
+    for (int idx = threadIdx.x; idx < (int)gridDim.x * KR; idx += RED_THREADS) v += __ldcg(part + idx);
+    sfin[threadIdx.x] = v;
+    __syncthreads();
     if (threadIdx.x < KR) {
       int j = threadIdx.x;
       double s = 0.0;
-      for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(part + (size_t)b * KR + j);
+      for (int t = j; t < RED_THREADS; t += KR) s += sfin[t];
       if (cs[j].active && !cs[j].done) cs[j].alpha = cs[j].rz / s;
     }
     if (threadIdx.x == 0) G->cntB = 0;
@@ -512,7 +689,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
 template <typename V, int KR>
 void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mode, ColState* cs, PcgGlobal* G,
                 double* part, cudaStream_t s) {
-  k_pcg_gather<V, KR><<<NPART, RED_THREADS, 0, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, Y, kp, p, z, mode, cs,
+  SG_LAUNCH k_pcg_gather<V, KR><<<NPART, RED_THREADS, 0, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, Y, kp, p, z, mode, cs,
                                                      G, part);
 }
 
@@ -547,7 +724,7 @@ template <typename V>
 void launch_gather_plain(const GatherTopo& T, int KR, const V* Y, V* out, int accumulate, const int* colmask,
                          cudaStream_t s) {
   int n = T.ngroups * KR;
-  if (n > 0) k_gather_plain<V><<<(n + 255) / 256, 256, 0, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, KR, Y, out,
+  if (n > 0) SG_LAUNCH k_gather_plain<V><<<(n + 255) / 256, 256, 0, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, KR, Y, out,
                                                                accumulate, colmask);
 }
 
@@ -611,16 +788,29 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
   }
   if (!last_block(&G->cntC)) return;
   __shared__ int s_alldone;
+  __shared__ double sfin[RED_THREADS];
   if (threadIdx.x == 0) s_alldone = 1;
+  // parallel fixed-order reduction of the block partials: thread t owns
+  // quantity t % (4*KR) of blocks t/(4*KR), t/(4*KR) + RED_THREADS/(4*KR), ...
+  {
+    constexpr int NQ = 4 * KR;
+    const int q = threadIdx.x % 4;
+    double v = 0.0;
+    for (int idx = threadIdx.x; idx < (int)gridDim.x * NQ; idx += RED_THREADS) {
+      double x = __ldcg(part + idx);
+      v = (q < 2) ? fmax(v, x) : v + x;
+    }
+    sfin[threadIdx.x] = v;
+  }
   __syncthreads();
   const int it = init ? 0 : G->it + 1;
   if (threadIdx.x < KR) {
     const int jj = threadIdx.x;
+    constexpr int NQ = 4 * KR;
     ColState& c = cs[jj];
     double a = 0.0, b = 0.0, s = 0.0, q = 0.0;
-    for (int blk = 0; blk < (int)gridDim.x; ++blk) {
-      const double* o = part + ((size_t)blk * KR + jj) * 4;
-      a = fmax(a, __ldcg(o)); b = fmax(b, __ldcg(o + 1)); s += __ldcg(o + 2); q += __ldcg(o + 3);
+    for (int t = jj * 4; t < RED_THREADS; t += NQ) {
+      a = fmax(a, sfin[t]); b = fmax(b, sfin[t + 1]); s += sfin[t + 2]; q += sfin[t + 3];
     }
     if (init) {
       if (c.active) {
@@ -653,7 +843,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
 template <typename V, int KR>
 void pcg_update(int n1, V* u, V* r, V* z, const V* p, const V* kp, const V* f, const V* dprecon, int init,
                 ColState* cs, PcgGlobal* G, double* part, cudaStream_t s) {
-  k_pcg_update<V, KR><<<NPART, RED_THREADS, 0, s>>>(n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
+  SG_LAUNCH k_pcg_update<V, KR><<<NPART, RED_THREADS, 0, s>>>(n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
 }
 
 // ---------------------------------------------------------------------------
@@ -875,7 +1065,7 @@ void launch_stress_update(const double* geo, const int* elist, int nel, const in
                           int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
                           double* fmax_part, cudaStream_t s) {
   // fixed grid so that fmax_part has NPART entries
-  k_stress_update<<<NPART, STRESS_WARPS * 32, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, xstride, xcol, mf, dt,
+  SG_LAUNCH k_stress_update<<<NPART, STRESS_WARPS * 32, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, xstride, xcol, mf, dt,
                                                        nl_isconv, finalize, evpt, stress, Yb, ystride, ycol,
                                                        fmax_part);
 }
@@ -884,8 +1074,8 @@ void launch_stress_update(const double* geo, const int* elist, int nel, const in
 // (accumulate = 1 adds to the existing stress, the elastic_stress_intact form).
 __global__ void k_elastic_stress(const double* __restrict__ geo, const int* __restrict__ elist, int nel,
                                  const int* __restrict__ ge, const int* __restrict__ mat_id,
-                                 const double* __restrict__ x, const MatF* __restrict__ mf, int accumulate,
-                                 double* __restrict__ stress) {
+                                 const double* __restrict__ x, int xstride, int xcol, const MatF* __restrict__ mf,
+                                 int accumulate, double* __restrict__ stress) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nel * NGLL) return;
   int le = t / NGLL, i = t - le * NGLL;
@@ -903,7 +1093,7 @@ __global__ void k_elastic_stress(const double* __restrict__ geo, const int* __re
     for (int c = 0; c < 3; ++c) {
       double s = 0.0;
 #pragma unroll
-      for (int mm = 0; mm < 3; ++mm) s = s + c_D[ic[a]][mm] * x[g[3 * (base + mm * stride) + c]];
+      for (int mm = 0; mm < 3; ++mm) s = s + c_D[ic[a]][mm] * x[(size_t)g[3 * (base + mm * stride) + c] * xstride + xcol];
       dU[c][a] = s;
     }
   }
@@ -924,10 +1114,11 @@ __global__ void k_elastic_stress(const double* __restrict__ geo, const int* __re
 }
 
 void launch_elastic_stress(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
-                           const double* x, const MatF* mf, int accumulate, double* stress, cudaStream_t s) {
+                           const double* x, int xstride, int xcol, const MatF* mf, int accumulate, double* stress,
+                           cudaStream_t s) {
   int n = nel * NGLL;
-  if (n > 0) k_elastic_stress<<<(n + 127) / 128, 128, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, mf, accumulate,
-                                                              stress);
+  if (n > 0) SG_LAUNCH k_elastic_stress<<<(n + 127) / 128, 128, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, xstride, xcol, mf,
+                                                              accumulate, stress);
 }
 
 // overburden_stress (src/postprocess.f90:10-33)
@@ -946,7 +1137,7 @@ __global__ void k_overburden(const double* __restrict__ g_coord, const int* __re
 void launch_overburden(const double* g_coord, const int* g_num, const int* mat_id, const double* gam, int nelmt,
                        double z0, double p0, double k0, double* stress, cudaStream_t s) {
   int n = nelmt * NGLL;
-  if (n > 0) k_overburden<<<(n + 255) / 256, 256, 0, s>>>(g_coord, g_num, mat_id, gam, nelmt, z0, p0, k0, stress);
+  if (n > 0) SG_LAUNCH k_overburden<<<(n + 255) / 256, 256, 0, s>>>(g_coord, g_num, mat_id, gam, nelmt, z0, p0, k0, stress);
 }
 
 // K9: equivalent nodal load of removed elements, sum_i B_i^T sigma_i detJ w
@@ -982,7 +1173,7 @@ __global__ void k_release_load(const double* __restrict__ geo, const int* __rest
 void launch_release_load(const double* geo, const int* elist, int nel, const int* mat_id, const double* gam,
                          const double* stress, double* Ye, cudaStream_t s) {
   int n = nel * NGLL;
-  if (n > 0) k_release_load<<<(n + 127) / 128, 128, 0, s>>>(geo, elist, nel, mat_id, gam, stress, Ye);
+  if (n > 0) SG_LAUNCH k_release_load<<<(n + 127) / 128, 128, 0, s>>>(geo, elist, nel, mat_id, gam, stress, Ye);
 }
 
 // ---------------------------------------------------------------------------
@@ -1014,7 +1205,7 @@ __global__ void k_nl_check(int n1, int KR, const double* __restrict__ x, double*
 
 void launch_nl_check(int n1, int KR, int k, const double* x, double* oldx, double* part, cudaStream_t s) {
   (void)k;
-  k_nl_check<<<NPART, RED_THREADS, 0, s>>>(n1, KR, x, oldx, part);
+  SG_LAUNCH k_nl_check<<<NPART, RED_THREADS, 0, s>>>(n1, KR, x, oldx, part);
 }
 
 // load = extload + bodyload; load(0) = 0 (src/slope.F90:288-289)
@@ -1029,7 +1220,7 @@ __global__ void k_load_combine(int n1, int KR, const double* __restrict__ ext, c
 
 void launch_load_combine(int n1, int KR, const double* extload, const double* bodyload, double* load,
                          cudaStream_t s) {
-  k_load_combine<<<NPART, RED_THREADS, 0, s>>>(n1, KR, extload, bodyload, load);
+  SG_LAUNCH k_load_combine<<<NPART, RED_THREADS, 0, s>>>(n1, KR, extload, bodyload, load);
 }
 
 // r64 = f - kp (FP64), r32 = (float) r64; partials |r|^2, |f|^2 per column.
@@ -1059,7 +1250,7 @@ __global__ void k_residual(int n1, int KR, const double* __restrict__ f, const d
 
 void launch_residual_norms(int n1, int KR, const double* f, const double* kp, double* r64, float* r32,
                            double* part, cudaStream_t s) {
-  k_residual<<<NPART, RED_THREADS, 0, s>>>(n1, KR, f, kp, r64, r32, part);
+  SG_LAUNCH k_residual<<<NPART, RED_THREADS, 0, s>>>(n1, KR, f, kp, r64, r32, part);
 }
 
 // x += d for the columns in colmask; partials max|d|, max|x| per column.
@@ -1093,7 +1284,7 @@ __global__ void k_axpy_corr(int n1, int KR, const int* __restrict__ colmask, con
 
 void launch_axpy_correction(int n1, int KR, const int* colmask, const float* d, double* x, double* part,
                             cudaStream_t s) {
-  k_axpy_corr<<<NPART, RED_THREADS, 0, s>>>(n1, KR, colmask, d, x, part);
+  SG_LAUNCH k_axpy_corr<<<NPART, RED_THREADS, 0, s>>>(n1, KR, colmask, d, x, part);
 }
 
 // dprecon(1:) = 1/dprecon(1:), dprecon(0) = 0 (src/slope.F90:199), plus an FP32 copy.
@@ -1106,7 +1297,7 @@ __global__ void k_invert_diag(int n1, double* __restrict__ dp, float* __restrict
 }
 
 void launch_invert_diag(int n1, double* dprecon, float* dprecon32, cudaStream_t s) {
-  k_invert_diag<<<(n1 + 255) / 256, 256, 0, s>>>(n1, dprecon, dprecon32);
+  SG_LAUNCH k_invert_diag<<<(n1 + 255) / 256, 256, 0, s>>>(n1, dprecon, dprecon32);
 }
 
 // explicit instantiations
@@ -1136,20 +1327,27 @@ template void launch_gather_plain<float>(const GatherTopo&, int, const float*, f
 // bit q of maxmask selects max instead of sum for quantity q.
 __global__ void k_final_reduce(const double* __restrict__ part, int nblk, int KR, int nq, int maxmask,
                                double* __restrict__ out) {
-  int t = threadIdx.x;
-  if (t >= KR * nq) return;
-  int q = t % nq;
-  bool mx = (maxmask >> q) & 1;
+  // thread t owns entry t % (KR*nq) of blocks t/(KR*nq), ...; 256 threads, KR*nq <= 64 divides 256
+  __shared__ double s[256];
+  const int W = KR * nq;
+  const int e = threadIdx.x % W, q = e % nq;
+  const bool mx = (maxmask >> q) & 1;
   double v = 0.0;
-  for (int b = 0; b < nblk; ++b) {
-    double x = part[(size_t)b * KR * nq + t];
+  for (int idx = threadIdx.x; idx < nblk * W; idx += blockDim.x) {
+    double x = part[idx];
     v = mx ? fmax(v, x) : v + x;
   }
-  out[t] = v;
+  s[threadIdx.x] = v;
+  __syncthreads();
+  if (threadIdx.x < W) {
+    double r = 0.0;
+    for (int t = threadIdx.x; t < (int)blockDim.x; t += W) r = mx ? fmax(r, s[t]) : r + s[t];
+    out[threadIdx.x] = r;
+  }
 }
 
 void launch_final_reduce(const double* part, int nblk, int KR, int nq, int maxmask, double* out, cudaStream_t s) {
-  k_final_reduce<<<1, 128, 0, s>>>(part, nblk, KR, nq, maxmask, out);
+  SG_LAUNCH k_final_reduce<<<1, 256, 0, s>>>(part, nblk, KR, nq, maxmask, out);
 }
 
 // Nodal displacement maxima of one column (src/slope.F90:400-415):
@@ -1180,13 +1378,25 @@ __global__ void k_disp_max(int nnode, const int* __restrict__ gdof, const double
 }
 
 void launch_disp_max(int nnode, const int* gdof, const double* x, int KR, int col, double* part, cudaStream_t s) {
-  k_disp_max<<<NPART, RED_THREADS, 0, s>>>(nnode, gdof, x, KR, col, part);
+  SG_LAUNCH k_disp_max<<<NPART, RED_THREADS, 0, s>>>(nnode, gdof, x, KR, col, part);
 }
 
 // x(:,col) /= n etc.: y[i*KR+col] = a*y[i*KR+col] (all columns when col < 0)
 __global__ void k_scale(size_t n, double* __restrict__ y, double a) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) y[i] = y[i] / a;
 }
-void launch_div(size_t n, double* y, double a, cudaStream_t s) { k_scale<<<NPART, RED_THREADS, 0, s>>>(n, y, a); }
+// zero column j of three [n1][KR] vectors (a new trial in slot j)
+__global__ void k_col_zero(int n1, int KR, int j, double* __restrict__ a, double* __restrict__ b,
+                           double* __restrict__ c) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += gridDim.x * blockDim.x) {
+    size_t o = (size_t)i * KR + j;
+    a[o] = 0.0; b[o] = 0.0; c[o] = 0.0;
+  }
+}
+void launch_col_zero(int n1, int KR, int j, double* a, double* b, double* c, cudaStream_t s) {
+  SG_LAUNCH k_col_zero<<<NPART, RED_THREADS, 0, s>>>(n1, KR, j, a, b, c);
+}
+
+void launch_div(size_t n, double* y, double a, cudaStream_t s) { SG_LAUNCH k_scale<<<NPART, RED_THREADS, 0, s>>>(n, y, a); }
 
 }  // namespace sg

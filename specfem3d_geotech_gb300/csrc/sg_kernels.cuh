@@ -40,6 +40,9 @@ struct MatF {
 };
 
 // Kernel launch wrappers (sg_kernels.cu)
+long long launch_count();        // kernel launches issued so far (host counter)
+void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline
+int apply_error_flag(cudaStream_t s);  // 1 if an apply kernel timed out on an mbarrier
 template <typename V, int KR>
 void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_old, const V* z, int combine,
                V* Y, const ColState* cs, const PcgGlobal* G, const int* d_nbr, cudaStream_t s);
@@ -56,7 +59,8 @@ void launch_stress_update(const double* geo, const int* elist, int nel, const in
                           int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
                           double* fmax_part, cudaStream_t s);
 void launch_elastic_stress(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
-                           const double* x, const MatF* mf, int accumulate, double* stress, cudaStream_t s);
+                           const double* x, int xstride, int xcol, const MatF* mf, int accumulate, double* stress,
+                           cudaStream_t s);
 void launch_overburden(const double* g_coord, const int* g_num, const int* mat_id, const double* gam, int nelmt,
                        double z0, double p0, double k0, double* stress, cudaStream_t s);
 void launch_release_load(const double* geo, const int* elist, int nel, const int* mat_id, const double* gam,
@@ -70,6 +74,7 @@ void launch_gather_plain(const GatherTopo& T, int KR, const V* Y, V* out, int ac
 void launch_final_reduce(const double* part, int nblk, int KR, int nq, int maxmask, double* out, cudaStream_t s);
 void launch_disp_max(int nnode, const int* gdof, const double* x, int KR, int col, double* part, cudaStream_t s);
 void launch_div(size_t n, double* y, double a, cudaStream_t s);
+void launch_col_zero(int n1, int KR, int j, double* a, double* b, double* c, cudaStream_t s);
 void launch_residual_norms(int n1, int KR, const double* f, const double* kp, double* r64, float* r32,
                            double* part, cudaStream_t s);
 void launch_axpy_correction(int n1, int KR, const int* colmask, const float* d, double* x, double* part,

@@ -1,11 +1,14 @@
 """GPU parity: the CUDA path through the C ABI against the CPU oracle.
 
-Tolerances: the FP64 path must match the oracle's displacement to relative
-L2 <= 1e-8 (the PCG step tolerance) with identical plastic-iteration counts.
-1e-8 and not 1e-9: the oracle itself moves by 5e-9 when only the summation
-order of its dot products changes (tests/test_oracle_kat.py::
-test_pcg_rounding_noise_floor), so a tighter bound would test rounding order,
-not the algorithm.  The mixed FP32/FP64 refinement form must stay within
+Tolerances: a single FP64 PCG solve must match the oracle's displacement to
+relative L2 <= 1e-8 (the PCG step tolerance); a whole plastic trial to 5e-8
+with identical plastic-iteration counts, 2e-6 on stresses and 2e-3 on fmax.
+These are twice the oracle's own rounding noise floor: the oracle moves by
+5e-9 (one solve) and 2.3e-8 / 5e-7 / 5e-4 (a trial's x / stress / fmax) when
+only the summation order of its dot products changes
+(tests/test_oracle_kat.py::test_pcg_rounding_noise_floor and
+test_trial_rounding_noise_floor), so tighter bounds would test rounding
+order, not the algorithm.  The mixed FP32/FP64 refinement form must stay within
 1e-6 of the FP64 result.  Integer outputs (node numbering, dof maps) must be
 identical.
 """
@@ -22,6 +25,9 @@ from specfem3d_geotech_gb300 import meshgen
 pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-8
+TRIAL_TOL = 5e-8
+STRESS_TOL = 2e-6
+FMAX_TOL = 2e-3
 MIXED_TOL = 1e-6
 
 
@@ -101,11 +107,12 @@ def test_trial_matches_oracle_fp64(ctx, slope):
         ro = om.trial(srf, want_x=True, want_stress=True)
         assert r["nl_iter"] == ro["nl_iter"] and r["converged"] == ro["converged"] == 1
         assert abs(r["cg_tot"] - ro["cg_tot"]) <= max(3, 0.01 * ro["cg_tot"])
-        assert rel(x[0], ro["x"]) <= FP64_TOL
+        assert rel(x[0], ro["x"]) <= TRIAL_TOL
         st = m.last_stress(0)
-        assert np.abs(st - ro["stress"]).max() <= 1e-8 * np.abs(ro["stress"]).max()
-        for key in ("uxmax", "umax", "fmax"):
-            assert abs(r[key] - ro[key]) <= 1e-8 * max(abs(ro[key]), 1e-12), key
+        assert np.abs(st - ro["stress"]).max() <= STRESS_TOL * np.abs(ro["stress"]).max()
+        for key in ("uxmax", "umax"):
+            assert abs(r[key] - ro[key]) <= TRIAL_TOL * abs(ro[key]), key
+        assert abs(r["fmax"] - ro["fmax"]) <= FMAX_TOL * abs(ro["fmax"])
 
 
 def test_golden_sweep_prefix(ctx):
@@ -118,7 +125,7 @@ def test_golden_sweep_prefix(ctx):
     for g in gold["trials"][:3]:
         r = m.trials([g["srf"]], ctl)[0]
         assert r["nl_iter"] == g["nl_iter"]
-        assert abs(r["umax"] - g["umax"]) <= 1e-8 * g["umax"]
+        assert abs(r["umax"] - g["umax"]) <= TRIAL_TOL * g["umax"]
 
 
 def test_deterministic_bitwise(ctx, slope):
@@ -139,7 +146,7 @@ def test_batched_trials_equal_single(ctx, slope):
     for t, s in enumerate(srfs):
         (r1,), x1 = m.trials([s], ctl, want_x=True)
         assert res[t]["nl_iter"] == r1["nl_iter"]
-        assert rel(xb[t], x1[0]) <= FP64_TOL
+        assert rel(xb[t], x1[0]) <= TRIAL_TOL
 
 
 def test_mixed_precision_within_tolerance(ctx, slope):
@@ -181,3 +188,54 @@ def test_excavation_matches_oracle(ctx):
     assert r.shape == ro.shape
     assert np.array_equal(r[:, 2], ro[:, 2])            # plastic iterations per stage
     assert np.allclose(r[:, 3:5], ro[:, 3:5], rtol=1e-8)  # uxmax, umax
+
+
+def test_tma_apply_matches_register_staged(ctx, slope, tmp_path):
+    """The TMA-pipelined element apply gives bitwise the same trial as the
+    register-staged one (same arithmetic, different data movement)."""
+    import subprocess
+    import sys
+    mesh, _ = slope
+    m = sg.Model(mesh, ctx=ctx)
+    _, x1 = m.trials([1.05], sg.make_control(), want_x=True)
+    out = tmp_path / "x0.npy"
+    code = ("import sys; sys.path.insert(0, %r); import numpy as np; import specfem3d_geotech_gb300 as sg;"
+            "from specfem3d_geotech_gb300 import meshgen; m = sg.Model(meshgen.slope2d());"
+            "_, x = m.trials([1.05], sg.make_control(), want_x=True); np.save(%r, x)") % (
+        os.path.dirname(os.path.dirname(os.path.abspath(__file__))), str(out))
+    env = dict(os.environ, SG_APPLY_VARIANT="0")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=300)
+    assert np.array_equal(np.load(out), x1)
+
+
+def test_continuous_batching_slot_refill(ctx, slope):
+    """A trial started in a slot freed by a finished trial gives the same
+    result as the trial run alone; so does a trial that ran in the mix."""
+    mesh, _ = slope
+    m = sg.Model(mesh, ctx=ctx)
+    ctl = sg.make_control()
+    alone = {s: m.trials([s], ctl)[0] for s in (1.0, 1.1, 1.05)}
+    m.batch_begin(ctl, 2)
+    a = m.batch_add(1.0)
+    b = m.batch_add(1.1)
+    c_started = False
+    res = {}
+    while True:
+        nlive = m.batch_step(1)
+        for slot in (a, b):
+            state, r = m.batch_poll(slot)
+            if state == 2 and r["srf"] not in res:
+                res[r["srf"]] = r
+                m.batch_release(slot)
+                if not c_started:
+                    m.batch_add(1.05)   # refills the freed slot while the other trial runs
+                    c_started = True
+        if nlive == 0 and c_started and len(res) == 3:
+            break
+        if nlive == 0 and len(res) >= 2 and not c_started:
+            break
+    m.batch_end()
+    assert set(res) == {1.0, 1.1, 1.05}
+    for s, r in res.items():
+        assert r["nl_iter"] == alone[s]["nl_iter"]
+        assert abs(r["umax"] - alone[s]["umax"]) <= TRIAL_TOL * alone[s]["umax"]

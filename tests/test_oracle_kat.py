@@ -202,3 +202,22 @@ def test_pcg_rounding_noise_floor():
     d = np.linalg.norm(sol[0][0] - sol[1][0]) / np.linalg.norm(sol[0][0])
     assert 1e-10 < d < 1e-8
     assert abs(sol[0][1] - sol[1][1]) <= 2
+
+
+def test_trial_rounding_noise_floor():
+    """A whole plastic trial (SRF 1.0, 12 plastic iterations) moves by ~2e-8 in x
+    and ~5e-7 in stress when only the dot-product summation order changes."""
+    om = OracleModel(meshgen.slope2d())
+    out = []
+    try:
+        for order in (0, 1):
+            L.orc_set_dot_order(order)
+            out.append(om.trial(1.0, want_x=True, want_stress=True))
+    finally:
+        L.orc_set_dot_order(0)
+    a, b = out
+    assert a["nl_iter"] == b["nl_iter"]
+    dx = np.linalg.norm(a["x"] - b["x"]) / np.linalg.norm(a["x"])
+    ds = np.abs(a["stress"] - b["stress"]).max() / np.abs(a["stress"]).max()
+    assert 1e-10 < dx < 5e-8
+    assert ds < 2e-6
