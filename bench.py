@@ -219,13 +219,54 @@ def run_reference(args, rank, world):
     return 0
 
 
+def plain_fp64(sg, ctx, mesh, srf0, args):
+    """Plain FP64 one-at-a-time trial on the same mesh: trial plastic iterations/s
+    and PCG iterations per plastic iteration of the reference algorithm."""
+    m64 = sg.Model(mesh, precision=sg.PREC_FP64, ctx=ctx)
+    c64 = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=NL_MAXITER)
+    m64.batch_begin(c64, 1)
+    m64.batch_add(srf0)
+    m64.batch_step(1)
+    b64 = m64.batch_poll(0)[1]
+    n64 = max(1, args.steps // 2)
+    ctx.mark(4)
+    m64.batch_step(n64)
+    ctx.mark(5)
+    t64 = ctx.elapsed_ms(4, 5)
+    a64 = m64.batch_poll(0)[1]
+    m64.batch_end()
+    m64.close()
+    steps64 = a64["nl_iter"] - b64["nl_iter"]
+    return steps64 / (t64 / 1000.0), (a64["cg_tot"] - b64["cg_tot"]) / max(1, steps64)
+
+
+def end_to_end(sg, ctx, mesh, ctl, srf, k, args, world):
+    """The same work through the public API from host buffers: mesh H2D +
+    device model build, the k trials for e2e_steps plastic iterations, result D2H."""
+    e2e_steps = max(1, args.steps // 2)
+    t0 = time.perf_counter()
+    me = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    me.batch_begin(ctl, k)
+    for s in srf:
+        me.batch_add(s)
+    me.batch_step(e2e_steps)
+    res = [me.batch_poll(t)[1] for t in range(k)]
+    me.batch_end()
+    t_e2e = time.perf_counter() - t0
+    me.close()
+    slot_steps = sum(r["nl_iter"] for r in res)
+    h2d = sum(a.nbytes for a in (mesh.x, mesh.y, mesh.z, mesh.conn, mesh.mat_id, mesh.props)) + \
+        sum(b.nbytes for b in mesh.bc)
+    return (slot_steps / t_e2e) * world / FOS_WORK, h2d, t_e2e, e2e_steps
+
+
 def run_ours(args, rank, world, local):
     import numpy as np
     import specfem3d_geotech_gb300 as sg
     from specfem3d_geotech_gb300 import build, meshgen
     build.build()
     ctx = sg.Context(local)
-    mesh = meshgen.slope3d(seed=1 + rank)
+    mesh = meshgen.slope3d(nx=args.nx, seed=1 + rank)
     k = args.k
     srf = [1.0 + 2.0 * (t + 1) / (k + 1) for t in range(k)]   # first k-section round on [1, 3]
 
@@ -258,10 +299,10 @@ def run_ours(args, rank, world, local):
     cg = sum(a["cg_tot"] - b["cg_tot"] for a, b in zip(after, before))
     model.batch_end()
     t_max = barrier_max(t_ms, world)
-    rate = slot_steps / (t_max / 1000.0)                       # trial plastic iterations / s (this rank)
-    rate_all = rate * world
+    rate_all = slot_steps / (t_max / 1000.0) * world         # trial plastic iterations / s, all ranks
     value = rate_all / FOS_WORK
     ne, neq = model.nelmt, model.neq
+    model.close()
 
     # roofline of the dominant kernel: the batched FP32 element apply (k RHS)
     hbm, peak_kind = peaks()
@@ -276,67 +317,42 @@ def run_ours(args, rank, world, local):
     if os.path.exists(tpath):
         with open(tpath) as f:
             traffic = json.load(f).get("bytes_per_launch")
-    model.close()
 
-    # ---- plain FP64 one-at-a-time form on the same mesh (the comparison) --
-    m64 = sg.Model(mesh, precision=sg.PREC_FP64, ctx=ctx)
-    c64 = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=NL_MAXITER)
-    m64.batch_begin(c64, 1)
-    m64.batch_add(srf[0])
-    m64.batch_step(1)
-    b64 = m64.batch_poll(0)[1]
-    n64 = max(1, args.steps // 2)
-    ctx.mark(4)
-    m64.batch_step(n64)
-    ctx.mark(5)
-    t64 = ctx.elapsed_ms(4, 5)
-    a64 = m64.batch_poll(0)[1]
-    m64.batch_end()
-    steps64 = a64["nl_iter"] - b64["nl_iter"]
-    rate64 = steps64 / (t64 / 1000.0)
-    n_cg_ref = (a64["cg_tot"] - b64["cg_tot"]) / max(1, steps64)
-    m64.close()
-
-    # ---- end to end through the public API with host buffers ------------
-    e2e_steps = max(1, args.steps // 2)
-    t0 = time.perf_counter()
-    me = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)     # H2D of the mesh + device build
-    me.batch_begin(ctl, k)
-    for s in srf:
-        me.batch_add(s)
-    me.batch_step(e2e_steps)
-    res = [me.batch_poll(t)[1] for t in range(k)]             # D2H of the results
-    me.batch_end()
-    t_e2e = time.perf_counter() - t0
-    me.close()
-    e2e_slot_steps = sum(r["nl_iter"] for r in res)
-    h2d = sum(a.nbytes for a in (mesh.x, mesh.y, mesh.z, mesh.conn, mesh.mat_id, mesh.props)) + \
-        sum(b.nbytes for b in mesh.bc)
-    e2e_value = (e2e_slot_steps / t_e2e) * world / FOS_WORK
+    if args.no_fp64:
+        rate64, n_cg_ref = float("nan"), N_CG_REF
+    else:
+        rate64, n_cg_ref = plain_fp64(sg, ctx, mesh, srf[0], args)
+        rate64 *= world
+    if args.no_e2e:
+        e2e = None
+    else:
+        e2e_value, h2d, t_e2e, e2e_steps = end_to_end(sg, ctx, mesh, ctl, srf, k, args, world)
+        e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
+               "d2h_bytes_per_step": k * 80 / e2e_steps, "seconds": t_e2e, "steps": e2e_steps}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": "slope3d_192k (120x40x40 hex, NGLL=3, 4.63M dof), mixed FP32/FP64-refined, "
-                               f"{k} concurrent SRF trials", "nelmt": ne, "neq": neq, "k_trials": k,
-                   "step": f"one plastic iteration of the {k}-trial batch",
+        "config": {"workload": f"slope3d_{ne // 1000}k ({args.nx}x40x40 hex, NGLL=3, {neq} dof), mixed "
+                               f"FP32/FP64-refined, {k} concurrent SRF trials", "nelmt": ne, "neq": neq,
+                   "k_trials": k, "step": f"one plastic iteration of the {k}-trial batch",
                    "fos_work_model": f"{FOS_TRIALS} trials x {NL_MAXITER} plastic iterations per FOS solve",
                    "l2": "inputs larger than L2 (FP32 element matrices 1.87 GB)", "parallelism": f"replicas{world}"},
         "trial_plastic_iters_per_s": rate_all,
         "pcg_iters_per_step": cg / max(1, args.steps),
-        "latency": {"step_p50_ms": float(np.percentile(step_ms, 50)), "step_p99_ms": float(np.percentile(step_ms, 99))},
-        "fp64_plain": {"trial_plastic_iters_per_s": rate64 * world, "value": rate64 * world / FOS_WORK,
+        "latency": {"step_p50_ms": float(np.percentile(step_ms, 50)),
+                    "step_p99_ms": float(np.percentile(step_ms, 99))},
+        "fp64_plain": {"trial_plastic_iters_per_s": rate64, "value": rate64 / FOS_WORK,
                        "pcg_iters_per_plastic_iter": n_cg_ref,
-                       "mixed_batched_over_plain": rate_all / (rate64 * world)},
+                       "mixed_batched_over_plain": rate_all / rate64 if rate64 == rate64 else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": f"k_apply_sparse_tma<float,{kr}>",
                      "algorithmic_bytes_per_launch": bytes_apply, "avg_launch_ms": apply_ms,
                      "peak_source": peak_kind},
         "gpu_launches": prof["launches"],
         "clocks": clk,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
-                "d2h_bytes_per_step": k * 80 / e2e_steps, "seconds": t_e2e, "steps": e2e_steps},
+        "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu:
         t0 = time.time()
@@ -348,7 +364,7 @@ def run_ours(args, rank, world, local):
                        f"{time.time() - t0:.0f} s), scaled by element count to 192k elements and to "
                        f"{n_cg_ref:.0f} PCG iterations per plastic iteration")}
     if rank == 0:
-        print(json.dumps(line))
+        print(json.dumps(line), flush=True)
     ctx.close()
     return 0
 
@@ -360,7 +376,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--k", type=int, default=K_TRIALS)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--nx", type=int, default=120, help="elements along x (120 = the 192k-element mesh)")
     args = ap.parse_args()
     rank, world, local = dist()
     if args.impl == "reference":

@@ -220,7 +220,7 @@ def test_continuous_batching_slot_refill(ctx, slope):
     b = m.batch_add(1.1)
     c_started = False
     res = {}
-    while True:
+    for _ in range(5000):
         nlive = m.batch_step(1)
         for slot in (a, b):
             state, r = m.batch_poll(slot)
