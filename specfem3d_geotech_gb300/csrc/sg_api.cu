@@ -91,7 +91,9 @@ struct sg_ctx {
   void release(void* p) {
     if (!p) return;
     auto it = live.find(p);
-    if (it != live.end()) { used -= it->second; live.erase(it); }
+    if (it == live.end()) return;  // not ours or already released
+    used -= it->second;
+    live.erase(it);
     cudaFree(p);
   }
   // profiling: events bracket the launches of one category
@@ -493,9 +495,10 @@ struct sg_model {
 static void model_release_work(sg_model* M) {
   sg_ctx* c = M->ctx;
   TrialWork& W = M->W;
+  // W.b64.Y aliases W.Yb and W.b32.part/cs/G alias the b64 ones: released once
   for (void* p : {(void*)W.x, (void*)W.oldx, (void*)W.load, (void*)W.bodyload, (void*)W.Yb, (void*)W.evpt,
                   (void*)W.stress, (void*)W.mf, (void*)W.b64.r, (void*)W.b64.z, (void*)W.b64.p, (void*)W.b64.kp,
-                  (void*)W.b64.Y, (void*)W.b64.part, (void*)W.b64.cs, (void*)W.b64.G, (void*)W.b32.r, (void*)W.b32.z,
+                  (void*)W.b64.part, (void*)W.b64.cs, (void*)W.b64.G, (void*)W.b32.r, (void*)W.b32.z,
                   (void*)W.b32.p, (void*)W.b32.kp, (void*)W.b32.Y, (void*)W.kp64, (void*)W.r64, (void*)W.r32,
                   (void*)W.d32, (void*)W.colmask, (void*)W.red})
     c->release(p);

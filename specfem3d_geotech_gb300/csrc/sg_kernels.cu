@@ -78,11 +78,38 @@ __device__ __forceinline__ double fmav<double>(double a, double b, double c) { r
 template <>
 __device__ __forceinline__ float fmav<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
-// p_new = z + beta*p, rounded the same way wherever it is formed.
+// p_new = z + beta*p, rounded the same way wherever it is formed (the apply
+// forms it on the fly, the gather stores it).  The FP32 solve stays in FP32
+// arithmetic: GB300's FP64 rate is 1/64 of its FP32 rate.
 template <typename V>
-__device__ __forceinline__ V pdir(double beta, V p, V z) {
-  return (V)fma(beta, (double)p, (double)z);
-}
+__device__ __forceinline__ V pdir(V beta, V p, V z) { return fmav<V>(beta, p, z); }
+
+// Dot-product accumulator.  FP64 vectors accumulate in FP64.  FP32 vectors
+// accumulate exact products (a*b = p + e with e = fma(a,b,-p)) in a
+// compensated two-float sum, which keeps FP64-level accuracy of the sum while
+// issuing only FP32 instructions; the pair is widened to FP64 per thread.
+template <typename V>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct DotAcc<float> {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    float t = hi + p;
+    float bp = t - hi;
+    float err = (hi - (t - bp)) + (p - bp);
+    hi = t;
+    lo += err + e;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 // Per-column block reduction of `val` (threads whose index = j mod KR hold
 // column j).  Result for column j lands in out[j] on thread 0..KR-1 of warp 0.
@@ -95,6 +122,28 @@ __device__ __forceinline__ double warp_col_reduce(double v, int op) {
     v = op ? fmax(v, w) : v + w;
   }
   return v;
+}
+
+
+// Load KR consecutive values (16-byte vector loads when the row allows it).
+template <typename V, int KR>
+__device__ __forceinline__ void loadv(const V* __restrict__ src, V (&out)[KR]) {
+  if constexpr (std::is_same<V, float>::value && KR % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < KR / 4; ++q) {
+      float4 t = reinterpret_cast<const float4*>(src)[q];
+      out[4 * q] = t.x; out[4 * q + 1] = t.y; out[4 * q + 2] = t.z; out[4 * q + 3] = t.w;
+    }
+  } else if constexpr (std::is_same<V, double>::value && KR % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < KR / 2; ++q) {
+      double2 t = reinterpret_cast<const double2*>(src)[q];
+      out[2 * q] = t.x; out[2 * q + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < KR; ++j) out[j] = src[j];
+  }
 }
 
 // last-block election: returns true in the block that finished last.
@@ -359,9 +408,9 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse(
   V* ks = wbase + warp * WSTRIDE;
   V* ps = ks + KS_STRIDE;
   for (int t = threadIdx.x; t < NGLL * KS_NBR; t += blockDim.x) nbr[t] = nbr_g[t];
-  double beta[KR];
+  V beta[KR];
 #pragma unroll
-  for (int j = 0; j < KR; ++j) beta[j] = combine ? cs[j].beta : 0.0;
+  for (int j = 0; j < KR; ++j) beta[j] = (V)(combine ? cs[j].beta : 0.0);
   __syncthreads();
   constexpr int NV = KS_STRIDE * (int)sizeof(V) / 16;
   for (int e = blockIdx.x * APPLY_WARPS + warp; e < nelmt; e += gridDim.x * APPLY_WARPS) {
@@ -477,9 +526,9 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
     mbar_init(bar + 1, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  double beta[KR];
+  V beta[KR];
 #pragma unroll
-  for (int j = 0; j < KR; ++j) beta[j] = combine ? cs[j].beta : 0.0;
+  for (int j = 0; j < KR; ++j) beta[j] = (V)(combine ? cs[j].beta : 0.0);
   __syncthreads();
   const int stride = gridDim.x * APPLY_WARPS;
   int e = blockIdx.x * APPLY_WARPS + warp;
@@ -498,12 +547,16 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         int g = ge[(size_t)e * NEDOF + 3 * lane + d];
+        V pv[KR];
+        loadv<V, KR>(pold + (size_t)g * KR, pv);
+        if (combine) {
+          V zv[KR];
+          loadv<V, KR>(z + (size_t)g * KR, zv);
 #pragma unroll
-        for (int j = 0; j < KR; ++j) {
-          V pv = pold[(size_t)g * KR + j];
-          if (combine) pv = pdir(beta[j], pv, z[(size_t)g * KR + j]);
-          ps[(3 * lane + d) * KR + j] = pv;
+          for (int j = 0; j < KR; ++j) pv[j] = pdir(beta[j], pv[j], zv[j]);
         }
+#pragma unroll
+        for (int j = 0; j < KR; ++j) ps[(3 * lane + d) * KR + j] = pv[j];
       }
     }
     bool ok = mbar_wait(bar + (i & 1), (unsigned)((i >> 1) & 1));
@@ -520,7 +573,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
 #pragma unroll
         for (int j = 0; j < KR; ++j) acc[c][j] = (V)0;
       const int* tb = nbr + lane * KS_NBR;
-#pragma unroll 1
+#pragma unroll
       for (int s = 0; s < KS_NBR; ++s) {
         int pk = tb[s];
         int m = pk & 31, kind = (pk >> 5) & 3, off = pk >> 8;
@@ -529,11 +582,13 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
         const V* pm = ps + 3 * m * KR;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
+          V pv[KR];
+          loadv<V, KR>(pm + d * KR, pv);
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             V kv = kb[c * sc + d * sd];
 #pragma unroll
-            for (int j = 0; j < KR; ++j) acc[c][j] = fmav<V>(kv, pm[d * KR + j], acc[c][j]);
+            for (int j = 0; j < KR; ++j) acc[c][j] = fmav<V>(kv, pv[j], acc[c][j]);
           }
         }
       }
@@ -612,14 +667,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
     const V* __restrict__ Y, V* __restrict__ kp, V* __restrict__ p, const V* __restrict__ z, int mode,
     ColState* __restrict__ cs, PcgGlobal* __restrict__ G, double* __restrict__ part) {
   if (G->all_done) return;
-  double dp[KR];
+  DotAcc<V> dacc[KR];
   bool live[KR];
-  double beta[KR];
+  V beta[KR];
 #pragma unroll
   for (int j = 0; j < KR; ++j) {
-    dp[j] = 0.0;
     live[j] = cs[j].active && !cs[j].done;
-    beta[j] = cs[j].beta;
+    beta[j] = (V)cs[j].beta;
   }
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
     V acc[3][KR];
@@ -631,9 +685,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
     for (int s = ptr[g]; s < s1; ++s) {
       const V* y = Y + (size_t)ent[s] * 3 * KR;
 #pragma unroll
-      for (int d = 0; d < 3; ++d)
+      for (int d = 0; d < 3; ++d) {
+        V yv[KR];
+        loadv<V, KR>(y + d * KR, yv);
 #pragma unroll
-        for (int j = 0; j < KR; ++j) acc[d][j] = acc[d][j] + y[d * KR + j];
+        for (int j = 0; j < KR; ++j) acc[d][j] = acc[d][j] + yv[j];
+      }
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -648,7 +705,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
           V pn = pdir(beta[j], p[o], z[o]);
           p[o] = pn;
           kp[o] = acc[d][j];
-          dp[j] += (double)pn * (double)acc[d][j];
+          dacc[j].add(pn, acc[d][j]);
         }
       }
     }
@@ -658,7 +715,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
   for (int j = 0; j < KR; ++j) {
-    double v = dp[j];
+    double v = dacc[j].value();
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
     if (lane == 0) sred[warp][j] = v;
@@ -743,8 +800,9 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
   if (G->all_done) return;
   const int j = threadIdx.x & (KR - 1);
   const bool live = cs[j].active && (init || !cs[j].done);
-  const double alpha = init ? 0.0 : cs[j].alpha;
-  double mp = 0.0, mu = 0.0, rz = 0.0, rr = 0.0;
+  const V alpha = (V)(init ? 0.0 : cs[j].alpha);
+  V mpv = (V)0, muv = (V)0;
+  DotAcc<V> rza, rra;
   if (live) {
     const size_t n = (size_t)n1 * KR;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -754,19 +812,20 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
         ri = f[i] - kp[i];
       } else {
         V pi = p[i];
-        V ui = (V)((double)u[i] + alpha * (double)pi);
+        V ui = fmav<V>(alpha, pi, u[i]);
         u[i] = ui;
-        mp = fmax(mp, fabs((double)pi));
-        mu = fmax(mu, fabs((double)ui));
-        ri = (V)((double)r[i] - alpha * (double)kp[i]);
+        mpv = fmax(mpv, fabs(pi));
+        muv = fmax(muv, fabs(ui));
+        ri = fmav<V>(-alpha, kp[i], r[i]);
       }
       V zi = dprecon[row] * ri;
       r[i] = ri;
       z[i] = zi;
-      rz += (double)ri * (double)zi;
-      rr += (double)ri * (double)ri;
+      rza.add(ri, zi);
+      rra.add(ri, ri);
     }
   }
+  double mp = (double)mpv, mu = (double)muv, rz = rza.value(), rr = rra.value();
   __shared__ double sred[RED_THREADS / 32][KR][4];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   mp = warp_col_reduce<KR>(mp, 1);
