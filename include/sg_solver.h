@@ -68,6 +68,24 @@ int sg_pcg_solve(sg_ctx* ctx, int neq, int nelmt, int nedof, const double* k, do
                  const double* f, const double* dprecon, const int* gdof_elmt, int cg_maxiter,
                  double cg_tol, int* cg_iter, char* errtag);
 
+/* No counterpart in the reference.  The same solve as sg_pcg_solve (same
+ * arguments and results, host arrays in and out) for callers that cannot
+ * allocate device memory -- code that runs under its own memory pool or
+ * sub-allocator, or that must not call cudaMalloc at all.  It needs no
+ * context: all device memory it uses is one static device array of 64 MiB
+ * held by every GPU that loads the library until the process exits, and it
+ * calls no cudaMalloc, cudaFree or other allocating routine.  Problems whose
+ * arrays need more than 64 MiB are rejected with SG_ERR_BADARG (the dense
+ * 81x81 FP64 element matrices alone take 52.5 KB per element, so about
+ * 1,100 elements fit).  The first call on a device looks up the array's
+ * device address; make it before any stream capture.  Calls share the
+ * array: each call clears what must start at zero, and calls that overlap on
+ * the GPU race and must be serialised by the caller.  Runs on the current
+ * device, on the legacy default stream, and returns when done. */
+int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double* k, double* u, const double* f,
+                         const double* dprecon, const int* gdof_elmt, int cg_maxiter, double cg_tol,
+                         int* cg_iter, char* errtag);
+
 /* ---- device-resident model -------------------------------------------- */
 /* Builds a spectral (27-node) model from an 8-node hex mesh: hex2spec with
  * node merging (src/mesh_spec.f90:17-386), face constraints and node-major dof

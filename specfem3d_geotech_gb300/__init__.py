@@ -36,7 +36,7 @@ EXPORTED = (
     "sg_model_from_hex8", "sg_model_from_deck", "sg_model_free", "sg_model_info", "sg_model_arrays",
     "sg_model_control", "sg_model_stiffness", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
-    "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms",
+    "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc",
 )
 
 
@@ -88,6 +88,8 @@ def lib(path: Optional[str] = None):
     L.sg_hbm_used.argtypes = [vp]
     L.sg_pcg_solve.restype = i
     L.sg_pcg_solve.argtypes = [vp, i, i, i, vp, vp, vp, vp, vp, i, d, C.POINTER(C.c_int), C.c_char_p]
+    L.sg_pcg_solve_noalloc.restype = i
+    L.sg_pcg_solve_noalloc.argtypes = [i, i, i, vp, vp, vp, vp, vp, i, d, C.POINTER(C.c_int), C.c_char_p]
     L.sg_model_from_hex8.restype = vp
     L.sg_model_from_hex8.argtypes = [vp, i, vp, vp, vp, i, vp, vp, i, vp, vp, vp, i, C.c_char_p]
     L.sg_model_from_deck.restype = vp
@@ -215,6 +217,31 @@ def pcg_solver(neq: int, nelmt: int, k: np.ndarray, u: np.ndarray, f: np.ndarray
                              cg_tol, C.byref(it), tag)
     if err not in (SG_OK, SG_ERR_NOCONV):
         raise SgError(err, tag.value.decode().strip() or ctx.last_error)
+    return it.value, err, tag.value.decode().rstrip()
+
+
+def pcg_solver_noalloc(neq: int, nelmt: int, k: np.ndarray, u: np.ndarray, f: np.ndarray, dprecon: np.ndarray,
+                       gdof_elmt: np.ndarray, cg_maxiter: int, cg_tol: float):
+    """:func:`pcg_solver` without any device allocation (sg_pcg_solve_noalloc).
+
+    For callers that cannot allocate device memory: everything the solve
+    needs on the GPU lives in the library's fixed 64 MiB static device array,
+    so there is no context and no cudaMalloc.  Larger problems raise
+    :class:`SgError` with SG_ERR_BADARG.  Calls must not overlap on the GPU.
+    Returns ``(cg_iter, errcode, errtag)`` like :func:`pcg_solver`.
+    """
+    if u.dtype != np.float64 or not u.flags.c_contiguous or u.shape[0] != neq + 1:
+        raise ValueError("u must be a C-contiguous float64 array of length neq+1")
+    k = np.ascontiguousarray(k, np.float64)
+    f = np.ascontiguousarray(f, np.float64)
+    dprecon = np.ascontiguousarray(dprecon, np.float64)
+    ge = np.ascontiguousarray(gdof_elmt, np.int32)
+    it = C.c_int(0)
+    tag = C.create_string_buffer(ERRTAG_LEN + 1)
+    err = lib().sg_pcg_solve_noalloc(neq, nelmt, 81, _ptr(k), _ptr(u), _ptr(f), _ptr(dprecon), _ptr(ge),
+                                     cg_maxiter, cg_tol, C.byref(it), tag)
+    if err not in (SG_OK, SG_ERR_NOCONV):
+        raise SgError(err, tag.value.decode().strip())
     return it.value, err, tag.value.decode().rstrip()
 
 
