@@ -128,7 +128,7 @@ typedef struct sg_control {
   int precision;       /* sg_precision */
   int reserved;
   double refine_rtol;  /* SG_PREC_MIXED: FP64 relative residual target (default 1e-10) */
-  double inner_rtol;   /* SG_PREC_MIXED: FP32 inner PCG residual reduction per refinement (default 1e-4) */
+  double inner_rtol;   /* SG_PREC_MIXED: FP32 residual reduction between FP64 residual replacements (default 1e-3) */
 } sg_control;
 
 typedef struct sg_trial_result {

@@ -246,7 +246,7 @@ def pcg_solver_noalloc(neq: int, nelmt: int, k: np.ndarray, u: np.ndarray, f: np
 
 
 def make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=2000, phinu=0, allelastic=0,
-                 precision=PREC_FP64, refine_rtol=1e-10, inner_rtol=1e-4) -> Control:
+                 precision=PREC_FP64, refine_rtol=1e-10, inner_rtol=1e-3) -> Control:
     return Control(cg_tol, nl_tol, cg_maxiter, nl_maxiter, phinu, allelastic, precision, 0, refine_rtol, inner_rtol)
 
 

@@ -153,7 +153,8 @@ struct PcgBufs {
 
 template <typename V, int KR>
 static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u, const V* f, const V* dp, int kcols,
-                     const int* active, int maxiter, double tol, int mode, int* iters, int* failed, int* used_iters) {
+                     const int* active, int maxiter, double tol, int mode, int* iters, int* failed, int* used_iters,
+                     double* laststep = nullptr) {
   cudaStream_t s = C->stream;
   ColState hcs[16];
   std::memset(hcs, 0, sizeof(hcs));
@@ -164,17 +165,33 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
   PcgGlobal hg;
   std::memset(&hg, 0, sizeof(hg));
   hg.maxiter = maxiter;
-  hg.mode = mode;
+  hg.mode = mode & 3;
   hg.kcols = kcols;
+  const bool keep_dir = (mode & 2) != 0;
+  if (keep_dir) {
+    // continue from the device-resident column state of the previous solve:
+    // only the activity mask and tolerances change
+    ColState prev[16];
+    cudaMemcpyAsync(prev, B.cs, sizeof(ColState) * KR, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (int j = 0; j < KR; ++j) {
+      prev[j].tol = hcs[j].tol;
+      prev[j].active = hcs[j].active;
+      hcs[j] = prev[j];
+    }
+  }
   cudaMemcpyAsync(B.cs, hcs, sizeof(ColState) * KR, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(B.G, &hg, sizeof(hg), cudaMemcpyHostToDevice, s);
-  cudaMemsetAsync(B.p, 0, sizeof(V) * (size_t)n1 * KR, s);
+  if (!keep_dir) cudaMemsetAsync(B.p, 0, sizeof(V) * (size_t)n1 * KR, s);
   cudaMemsetAsync(B.kp, 0, sizeof(V) * (size_t)n1 * KR, s);
-  int ev = C->prof_begin();
-  pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, u, (const V*)nullptr, 0, B.Y, B.cs, B.G, C->d_nbr, s);
-  C->prof_end(ev, 1);
+  int ev;
+  if (!(mode & 4)) {  // bit 2: the caller guarantees u = 0, so kp = K u = 0 without an apply
+    ev = C->prof_begin();
+    pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, u, (const V*)nullptr, 0, B.Y, B.cs, B.G, C->d_nbr, s);
+    C->prof_end(ev, 1);
+    pcg_gather<V, KR>(*op.T, B.Y, B.kp, B.p, B.z, 0, B.cs, B.G, B.part, s);
+  }
   ev = C->prof_begin();
-  pcg_gather<V, KR>(*op.T, B.Y, B.kp, B.p, B.z, 0, B.cs, B.G, B.part, s);
   pcg_update<V, KR>(n1, u, B.r, B.z, B.p, B.kp, f, dp, 1, B.cs, B.G, B.part, s);
   C->prof_end(ev, 3);
   const int chunk = op.nelmt >= 50000 ? 4 : (op.nelmt >= 5000 ? 16 : 64);
@@ -206,6 +223,7 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
   for (int j = 0; j < kcols; ++j) {
     iters[j] = hcs[j].iters;
     failed[j] = hcs[j].failed;
+    if (laststep) laststep[j] = std::fabs(hcs[j].alpha) * hcs[j].maxp;
     if (hcs[j].active && hcs[j].failed && status == SG_OK) status = SG_ERR_NOCONV;
   }
   if (used_iters) *used_iters = it;
@@ -216,13 +234,13 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
 template <typename V>
 static int pcg_run(sg_ctx* C, int KR, const Op& op, const PcgBufs<V>& B, int n1, V* u, const V* f, const V* dp,
                    int kcols, const int* active, int maxiter, double tol, int mode, int* iters, int* failed,
-                   int* used) {
+                   int* used, double* laststep = nullptr) {
   switch (KR) {
-    case 1: return pcg_run_t<V, 1>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
-    case 2: return pcg_run_t<V, 2>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
-    case 4: return pcg_run_t<V, 4>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
-    case 8: return pcg_run_t<V, 8>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
-    case 16: return pcg_run_t<V, 16>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used);
+    case 1: return pcg_run_t<V, 1>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used, laststep);
+    case 2: return pcg_run_t<V, 2>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used, laststep);
+    case 4: return pcg_run_t<V, 4>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used, laststep);
+    case 8: return pcg_run_t<V, 8>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used, laststep);
+    case 16: return pcg_run_t<V, 16>(C, op, B, n1, u, f, dp, kcols, active, maxiter, tol, mode, iters, failed, used, laststep);
   }
   return SG_ERR_BADARG;
 }
@@ -832,11 +850,15 @@ static int linear_solve(sg_model* M, const sg_control* ctl, const Op& op64, cons
     return st;
   }
   const double rtol = ctl->refine_rtol > 0 ? ctl->refine_rtol : 1e-10;
-  const double itol = ctl->inner_rtol > 0 ? ctl->inner_rtol : 1e-4;
+  const double itol = ctl->inner_rtol > 0 ? ctl->inner_rtol : 1e-3;
   std::vector<int> live(active);
   std::vector<int> step_ok(k, 0);
   double red[64];
-  for (int round = 0; round < 60; ++round) {
+  // Reliable-update mixed CG: the FP32 PCG on K32 keeps its search direction
+  // across rounds; each round ends when its recursive residual has dropped by
+  // itol, the correction is added to the FP64 solution, and the FP32 residual
+  // is replaced by the true residual f - K64 x computed in FP64.
+  for (int round = 0; round < 200; ++round) {
     apply_plain<double>(c, KR, op64, W.x, W.Yb, W.kp64);
     launch_residual_norms(n1, KR, W.load, W.kp64, W.r64, W.r32, W.b64.part, c->stream);
     reduce_read(c, W.b64.part, NPART, KR, 2, 0, W.red, red);
@@ -851,13 +873,16 @@ static int linear_solve(sg_model* M, const sg_control* ctl, const Op& op64, cons
       else any = true;
     }
     if (!any) return SG_OK;
-    // inner FP32 solve K d = r for the live columns
+    // round 0 starts the FP32 PCG; later rounds continue its search direction
+    // (all live columns enter a solve together, so they share the round structure)
     cudaMemsetAsync(W.d32, 0, sizeof(float) * (size_t)n1 * KR, c->stream);
-    int it[16], fl[16], used = 0;
-    int st = pcg_run<float>(c, KR, op32, W.b32, n1, W.d32, W.r32, dprecon32, k, live.data(), ctl->cg_maxiter,
-                            itol, 1, it, fl, &used);
-    if (st != SG_OK && st != SG_ERR_NOCONV) return st;
+    int it[16] = {0}, fl[16] = {0}, used = 0;
+    (void)fl;
+    double step[16] = {0};
     int mask[16] = {0};
+    int st = pcg_run<float>(c, KR, op32, W.b32, n1, W.d32, W.r32, dprecon32, k, live.data(), ctl->cg_maxiter, itol,
+                            (round == 0 ? 1 : 3) | 4, it, fl, &used, step);
+    if (st != SG_OK && st != SG_ERR_NOCONV) return st;
     for (int j = 0; j < k; ++j) {
       mask[j] = live[j];
       if (live[j]) S.iters[j] += it[j];
@@ -865,8 +890,9 @@ static int linear_solve(sg_model* M, const sg_control* ctl, const Op& op64, cons
     cudaMemcpyAsync(W.colmask, mask, sizeof(int) * 16, cudaMemcpyHostToDevice, c->stream);
     launch_axpy_correction(n1, KR, W.colmask, W.d32, W.x, W.b64.part, c->stream);
     reduce_read(c, W.b64.part, NPART, KR, 2, 3, W.red, red);
+    // the reference's step test on the last CG step: |alpha|*max|p| <= cg_tol*max|x|
     for (int j = 0; j < k; ++j)
-      if (live[j]) step_ok[j] = (red[2 * j + 1] > 0) && (red[2 * j] / red[2 * j + 1] <= ctl->cg_tol);
+      if (live[j]) step_ok[j] = (red[2 * j + 1] > 0) && (step[j] <= ctl->cg_tol * red[2 * j + 1]);
   }
   c->err = "iterative refinement did not converge";
   return SG_ERR_NOCONV;

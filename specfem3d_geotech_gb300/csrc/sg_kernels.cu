@@ -873,13 +873,16 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
     }
     if (init) {
       if (c.active) {
-        c.rz = s; c.rr0 = q; c.rr = q; c.beta = 0.0; c.done = 0; c.failed = 0; c.iters = 0;
+        // keep_dir (G->mode & 2): continue the previous search direction after a
+        // residual replacement, beta = r.z_new / r.z of the last completed step
+        c.beta = (G->mode & 2) ? s / c.rz : 0.0;
+        c.rz = s; c.rr0 = q; c.rr = q; c.done = 0; c.failed = 0; c.iters = 0;
       } else {
         c.done = 1;
       }
     } else if (c.active && !c.done) {
       c.maxp = a; c.maxu = b; c.rr = q;
-      bool stop = (G->mode == 0) ? (fabs(c.alpha) * a / b <= c.tol) : (q <= c.tol * c.tol * c.rr0);
+      bool stop = ((G->mode & 1) == 0) ? (fabs(c.alpha) * a / b <= c.tol) : (q <= c.tol * c.tol * c.rr0);
       if (stop) {
         c.done = 1; c.iters = it;
       } else if (it >= G->maxiter) {

@@ -25,7 +25,7 @@ struct PcgGlobal {
   int all_done;
   int it;         // iterations completed
   int maxiter;
-  int mode;       // 0 = reference step test, 1 = residual reduction test
+  int mode;       // bit 0: 0 = reference step test, 1 = residual reduction test; bit 1: keep direction
   int kcols;      // columns in use (<= KR)
   unsigned cntB, cntC, pad;
 };

@@ -239,3 +239,29 @@ def test_continuous_batching_slot_refill(ctx, slope):
     for s, r in res.items():
         assert r["nl_iter"] == alone[s]["nl_iter"]
         assert abs(r["umax"] - alone[s]["umax"]) <= TRIAL_TOL * alone[s]["umax"]
+
+
+def test_sweep_critical_srf_matches_golden(ctx):
+    """The slope3d SRF sweep 1.00:0.05:2.00 on the 300-element slope stops at the
+    oracle's critical SRF (1.35) with the oracle's plastic-iteration counts."""
+    path = os.path.join(os.path.dirname(__file__), "golden", "slope2d_sweep.json")
+    with open(path) as f:
+        gold = json.load(f)
+    mesh = meshgen.slope2d()
+    m = sg.Model(mesh, ctx=ctx)
+    res = m.sweep(list(mesh.control.srf), sg.make_control())
+    assert [r["srf"] for r in res] == [g["srf"] for g in gold["trials"]]
+    assert res[-1]["failed"] == 1 and res[-1]["srf"] == gold["critical_srf"]
+    for r, g in zip(res, gold["trials"]):
+        assert r["nl_iter"] == g["nl_iter"] and r["failed"] == g["failed"]
+        if not g["failed"]:
+            assert abs(r["umax"] - g["umax"]) <= TRIAL_TOL * g["umax"]
+
+
+def test_fos_mixed_batched_matches_oracle_critical_srf(ctx):
+    """Mixed precision, 8 concurrent trials per k-section round: same critical SRF."""
+    mesh = meshgen.slope2d()
+    m = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    fos, ntrials, nrounds = m.fos(sg.make_control(precision=sg.PREC_MIXED), lo=1.0, hi=2.0, step=0.05, k=8)
+    assert abs(fos - 1.35) < 1e-12
+    assert nrounds <= 3
