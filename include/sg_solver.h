@@ -182,6 +182,33 @@ int sg_srf_sweep(sg_model* model, const sg_control* ctl, int nsrf, const double*
 int sg_fos(sg_model* model, const sg_control* ctl, double lo, double hi, double step, int k,
            double* fos, int* ntrials, int* nrounds);
 
+/* ---- request loop: factor-of-safety solves of many meshes ---------------
+ * Requests are queued on submission and admitted in arrival order when their
+ * estimated HBM footprint fits the server's budget (hbm_budget = 0: 90 % of
+ * free device memory).  `workers` threads each own a context and stream, so
+ * admitted requests run concurrently on the device; inside a request the SRF
+ * search is sg_fos with k batched trials.  Times are seconds since the server
+ * was created. */
+typedef struct sg_server sg_server;
+typedef struct sg_fos_result {
+  int id, status;
+  double fos;
+  int ntrials, nrounds, nelmt, neq;
+  double footprint, hbm_bytes;        /* admission estimate, device bytes used */
+  double t_arrival, t_start, t_done;
+} sg_fos_result;
+sg_server* sg_server_create(int device, size_t hbm_budget, int workers);
+int sg_server_submit(sg_server* server, int nnode8, const double* x8, const double* y8, const double* z8,
+                     int nelmt, const int* conn8, const int* mat_id, int nmatblk, const double* props,
+                     const int* bc_counts, const int* bc_pairs, const sg_control* ctl, double lo,
+                     double hi, double step, int k, int* id);
+/* Blocks until request `id` is done (or timeout_s passes: SG_ERR_TIMEOUT). */
+int sg_server_wait(sg_server* server, int id, double timeout_s, sg_fos_result* result);
+/* stats[0..5] = completed, p50 latency, p99 latency (arrival to done, s),
+ * completed / (last done - first arrival), peak concurrent requests, budget bytes. */
+int sg_server_stats(sg_server* server, double* stats);
+void sg_server_destroy(sg_server* server);
+
 /* ---- staged excavation (src/excavation.F90:15-709), nsrf = 1 ---------- */
 /* s0_type 1: overburden initial stress s0 - gamma*|z - z0| with K0
  * (src/postprocess.f90:10-33); s0_type 0: elastic gravity solve

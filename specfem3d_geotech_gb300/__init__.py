@@ -37,6 +37,7 @@ EXPORTED = (
     "sg_model_control", "sg_model_stiffness", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
     "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc",
+    "sg_server_create", "sg_server_submit", "sg_server_wait", "sg_server_stats", "sg_server_destroy",
 )
 
 
@@ -52,6 +53,18 @@ class Control(C.Structure):
     _fields_ = [("cg_tol", C.c_double), ("nl_tol", C.c_double), ("cg_maxiter", C.c_int), ("nl_maxiter", C.c_int),
                 ("phinu", C.c_int), ("allelastic", C.c_int), ("precision", C.c_int), ("reserved", C.c_int),
                 ("refine_rtol", C.c_double), ("inner_rtol", C.c_double)]
+
+
+class FosResult(C.Structure):
+    """sg_fos_result (include/sg_solver.h)."""
+
+    _fields_ = [("id", C.c_int), ("status", C.c_int), ("fos", C.c_double), ("ntrials", C.c_int),
+                ("nrounds", C.c_int), ("nelmt", C.c_int), ("neq", C.c_int), ("footprint", C.c_double),
+                ("hbm_bytes", C.c_double), ("t_arrival", C.c_double), ("t_start", C.c_double),
+                ("t_done", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class TrialResult(C.Structure):
@@ -130,6 +143,16 @@ def lib(path: Optional[str] = None):
     L.sg_batch_release.argtypes = [vp, i]
     L.sg_batch_end.restype = i
     L.sg_batch_end.argtypes = [vp]
+    L.sg_server_create.restype = vp
+    L.sg_server_create.argtypes = [i, sz, i]
+    L.sg_server_submit.restype = i
+    L.sg_server_submit.argtypes = [vp, i, vp, vp, vp, i, vp, vp, i, vp, vp, vp, C.POINTER(Control), d, d, d, i,
+                                   C.POINTER(C.c_int)]
+    L.sg_server_wait.restype = i
+    L.sg_server_wait.argtypes = [vp, i, d, C.POINTER(FosResult)]
+    L.sg_server_stats.restype = i
+    L.sg_server_stats.argtypes = [vp, vp]
+    L.sg_server_destroy.argtypes = [vp]
     L.sg_timer_mark.restype = i
     L.sg_timer_mark.argtypes = [vp, i]
     L.sg_timer_ms.restype = d
@@ -402,3 +425,48 @@ class Model:
         if st:
             raise SgError(st, self.ctx.last_error)
         return res.reshape(-1, 8)[: n.value]
+
+
+class Server:
+    """sg_server: a request loop of factor-of-safety solves (see include/sg_solver.h)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, workers: int = 4):
+        self.h = lib().sg_server_create(device, hbm_budget, workers)
+        if not self.h:
+            raise SgError(SG_ERR_NODEVICE, "sg_server_create failed")
+        self._keep = {}
+
+    def submit(self, mesh, ctl: Control, lo: float = 1.0, hi: float = 3.0, step: float = 0.01, k: int = 8) -> int:
+        arrs = [np.ascontiguousarray(mesh.x, np.float64), np.ascontiguousarray(mesh.y, np.float64),
+                np.ascontiguousarray(mesh.z, np.float64), np.ascontiguousarray(mesh.conn.reshape(-1), np.int32),
+                np.ascontiguousarray(mesh.mat_id, np.int32), np.ascontiguousarray(mesh.props.reshape(-1), np.float64),
+                np.array([b.shape[0] for b in mesh.bc], np.int32),
+                np.ascontiguousarray(np.concatenate(mesh.bc).reshape(-1), np.int32)]
+        x, y, z, conn, mid, props, cnt, pairs = arrs
+        rid = C.c_int(0)
+        st = lib().sg_server_submit(self.h, mesh.nnode8, _ptr(x), _ptr(y), _ptr(z), mesh.nelmt, _ptr(conn), _ptr(mid),
+                                    mesh.props.shape[0], _ptr(props), _ptr(cnt), _ptr(pairs), C.byref(ctl), lo, hi,
+                                    step, k, C.byref(rid))
+        if st:
+            raise SgError(st, "sg_server_submit")
+        return rid.value
+
+    def wait(self, rid: int, timeout: float = 3600.0):
+        r = FosResult()
+        st = lib().sg_server_wait(self.h, rid, timeout, C.byref(r))
+        if st:
+            raise SgError(st, "sg_server_wait")
+        return r.as_dict()
+
+    def stats(self):
+        o = np.zeros(6)
+        lib().sg_server_stats(self.h, _ptr(o))
+        return dict(completed=int(o[0]), p50_s=o[1], p99_s=o[2], solves_per_s=o[3], peak_concurrent=int(o[4]),
+                    budget_bytes=o[5])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sg_server_destroy(self.h)
+            self.h = None
+
+    __del__ = close
