@@ -187,7 +187,7 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
   int ev;
   if (!(mode & 4)) {  // bit 2: the caller guarantees u = 0, so kp = K u = 0 without an apply
     ev = C->prof_begin();
-    pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, u, (const V*)nullptr, 0, B.Y, B.cs, B.G, C->d_nbr, s);
+    pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, u, (const V*)nullptr, 0, B.Y, B.cs, B.G, C->d_nbr, op.T->d_pos, s);
     C->prof_end(ev, 1);
     pcg_gather<V, KR>(*op.T, B.Y, B.kp, B.p, B.z, 0, B.cs, B.G, B.part, s);
   }
@@ -202,7 +202,7 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
   while (true) {
     for (int c = 0; c < chunk; ++c) {
       ev = C->prof_begin();
-      pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, B.p, B.z, 1, B.Y, B.cs, B.G, C->d_nbr, s);
+      pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, B.p, B.z, 1, B.Y, B.cs, B.G, C->d_nbr, op.T->d_pos, s);
       C->prof_end(ev, 1);
       ev = C->prof_begin();
       pcg_gather<V, KR>(*op.T, B.Y, B.kp, B.p, B.z, 1, B.cs, B.G, B.part, s);
@@ -251,11 +251,11 @@ template <typename V>
 static void apply_plain(sg_ctx* C, int KR, const Op& op, const V* x, V* Y, V* out) {
   int ev = C->prof_begin();
   switch (KR) {
-    case 1: pcg_apply<V, 1>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
-    case 2: pcg_apply<V, 2>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
-    case 4: pcg_apply<V, 4>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
-    case 8: pcg_apply<V, 8>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
-    case 16: pcg_apply<V, 16>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, C->stream); break;
+    case 1: pcg_apply<V, 1>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
+    case 2: pcg_apply<V, 2>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
+    case 4: pcg_apply<V, 4>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
+    case 8: pcg_apply<V, 8>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
+    case 16: pcg_apply<V, 16>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
   }
   C->prof_end(ev, 1);
   ev = C->prof_begin();
@@ -306,8 +306,8 @@ sg_ctx* sg_create(int device, size_t hbm_budget) {
 int sg_create_status(void) { return g_create_status; }
 
 static void free_topo(sg_ctx* c, GatherTopo& T) {
-  c->release(T.d_ptr); c->release(T.d_ent); c->release(T.d_dof);
-  T.d_ptr = T.d_ent = T.d_dof = nullptr;
+  c->release(T.d_ptr); c->release(T.d_ent); c->release(T.d_dof); c->release(T.d_pos);
+  T.d_ptr = T.d_ent = T.d_dof = T.d_pos = nullptr;
 }
 
 static bool upload_topo(sg_ctx* c, GatherTopo& T) {
@@ -315,7 +315,9 @@ static bool upload_topo(sg_ctx* c, GatherTopo& T) {
   T.d_ptr = c->alloc<int>(T.ptr.size());
   T.d_ent = c->alloc<int>(T.ent.size());
   T.d_dof = c->alloc<int>(T.dof.size());
-  if (!T.d_ptr || !T.d_ent || !T.d_dof) return false;
+  T.d_pos = c->alloc<int>(T.pos.size());
+  if (!T.d_ptr || !T.d_ent || !T.d_dof || !T.d_pos) return false;
+  if (!T.pos.empty()) cudaMemcpyAsync(T.d_pos, T.pos.data(), sizeof(int) * T.pos.size(), cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(T.d_ptr, T.ptr.data(), sizeof(int) * T.ptr.size(), cudaMemcpyHostToDevice, c->stream);
   if (!T.ent.empty()) cudaMemcpyAsync(T.d_ent, T.ent.data(), sizeof(int) * T.ent.size(), cudaMemcpyHostToDevice, c->stream);
   if (!T.dof.empty()) cudaMemcpyAsync(T.d_dof, T.dof.data(), sizeof(int) * T.dof.size(), cudaMemcpyHostToDevice, c->stream);
@@ -569,7 +571,7 @@ static bool model_stiffness(sg_model* M, const int* d_elist, int nel, const doub
   double* Ygrav = M->d_Yscratch + (size_t)M->H.nelmt * NEDOF;
   int ev = c->prof_begin();
   launch_stiffness(M->d_geo, M->d_matid, d_elist, nel, M->d_ym, d_nuv, M->d_gam, M->d_K64, M->d_K32, Ydiag,
-                   gravity ? Ygrav : nullptr, c->d_entry, s);
+                   gravity ? Ygrav : nullptr, c->d_entry, T.d_pos, s);
   c->prof_end(ev, 5);
   cudaMemsetAsync(M->d_diag, 0, sizeof(double) * n1, s);
   launch_gather_plain<double>(T, 1, Ydiag, M->d_diag, 0, nullptr, s);
@@ -1059,7 +1061,7 @@ static int batch_iteration(sg_model* M) {
     fin[t] = conv[t] || S.res.nl_iter == ctl->nl_maxiter;
     int ev = c->prof_begin();
     launch_stress_update(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, W.x, KR, t, W.mf + (size_t)t * h.nmatblk, S.dt,
-                         conv[t], fin[t], W.evpt + nst * t, W.stress + nst * t, W.Yb, KR, t, M->d_fpart, s);
+                         conv[t], fin[t], W.evpt + nst * t, W.stress + nst * t, W.Yb, KR, t, M->d_fpart, M->T.d_pos, s);
     c->prof_end(ev, 4);
     reduce_read(c, M->d_fpart, NPART, 1, 1, 1, W.red, red + 32);
     S.res.fmax = red[32];
@@ -1329,7 +1331,7 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
         double* Ye = M->d_Yscratch;
         cudaMemsetAsync(M->d_extload, 0, sizeof(double) * n1, s);
         if (nvoid) {
-          launch_release_load(M->d_geo, d_evoid, nvoid, M->d_matid, M->d_gam, stress, Ye, s);
+          launch_release_load(M->d_geo, d_evoid, nvoid, M->d_matid, M->d_gam, stress, Ye, Tv.d_pos, s);
           launch_gather_plain<double>(Tv, 1, Ye, M->d_extload, 0, nullptr, s);
         }
         launch_div((size_t)n1, M->d_extload, (double)ninc, s);
@@ -1365,7 +1367,7 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
             double uerr = red[0] / red[1];
             int conv = uerr <= ctl->nl_tol, fin = conv || nl_iter == ctl->nl_maxiter;
             launch_stress_update(M->d_geo, d_eint, nint, d_geall, M->d_matid, W.x, 1, 0, W.mf, dt, conv, fin, evpt,
-                                 stress, W.Yb, 1, 0, M->d_fpart, s);
+                                 stress, W.Yb, 1, 0, M->d_fpart, Ti.d_pos, s);
             reduce_read(c, M->d_fpart, NPART, 1, 1, 1, W.red, red);
             fmax = red[0];
             if (!fin) launch_gather_plain<double>(Ti, 1, W.Yb, W.bodyload, 1, nullptr, s);

@@ -182,11 +182,13 @@ void build_groups_from_gdof(const int* ge, int nelmt, int neq, GatherTopo& T) {
   for (int g = 0; g < ng; ++g) T.ptr[g + 1] += T.ptr[g];
   T.ent.assign(T.ptr[ng], 0);
   T.dof.assign((size_t)3 * ng, 0);
+  T.pos.assign((size_t)nelmt * NGLL, -1);
   std::vector<int> fill(T.ptr.begin(), T.ptr.end() - 1);
   for (size_t s = 0; s < (size_t)nelmt * NGLL; ++s) {
     int k = key[s];
     if (!k) continue;
     int g = gid[k];
+    T.pos[s] = fill[g];
     T.ent[fill[g]++] = (int)s;
     for (int d = 0; d < 3; ++d) T.dof[(size_t)3 * g + d] = ge[3 * s + d];
   }

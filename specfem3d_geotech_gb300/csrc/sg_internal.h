@@ -45,7 +45,8 @@ struct Profile {
 struct GatherTopo {
   int ngroups = 0;
   std::vector<int> ptr, ent, dof;  // host copies
-  int *d_ptr = nullptr, *d_ent = nullptr, *d_dof = nullptr;
+  std::vector<int> pos;            // slot -> position in ent (-1: node with no free dof)
+  int *d_ptr = nullptr, *d_ent = nullptr, *d_dof = nullptr, *d_pos = nullptr;
 };
 
 // Host-side spectral model (the reference's global arrays).
@@ -93,7 +94,7 @@ void launch_geometry(const double* g_coord, const int* g_num, int nelmt, double*
 // per element, both gathered later into global vectors.
 void launch_stiffness(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
                       const double* nu, const double* gam, double* Ks64, float* Ks32, double* Ydiag,
-                      double* Ygrav, const int* d_entry, cudaStream_t s);
+                      double* Ygrav, const int* d_entry, const int* pos, cudaStream_t s);
 void launch_expand_dense(const double* Ks64, int nel, double* dense, const int* d_entry, cudaStream_t s);
 
 }  // namespace sg

@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(STIFF_THREADS) k_stiffness(
     const double* __restrict__ geo, const int* __restrict__ mat_id, const int* __restrict__ elist, int nel,
     const double* __restrict__ ym, const double* __restrict__ nu, const double* __restrict__ gam,
     double* __restrict__ Ks64, float* __restrict__ Ks32, double* __restrict__ Ydiag, double* __restrict__ Ygrav,
-    const int* __restrict__ entry) {
+    const int* __restrict__ entry, const int* __restrict__ pos) {
   __shared__ double sg[NGLL][NGLL][3];   // grad of node n at point i (zero off the lines)
   __shared__ double sgeo[NGLL][GEO_STRIDE];
   __shared__ double swd[NGLL];
@@ -297,7 +297,10 @@ __global__ void __launch_bounds__(STIFF_THREADS) k_stiffness(
     size_t o = (size_t)le * KS_STRIDE + t;
     if (Ks64) Ks64[o] = acc;
     if (Ks32) Ks32[o] = (float)acc;
-    if (row == col && Ydiag) Ydiag[(size_t)le * NEDOF + row] = acc;
+    if (row == col && Ydiag) {
+      int ps = pos[(size_t)le * NGLL + row / 3];
+      if (ps >= 0) Ydiag[(size_t)ps * 3 + row % 3] = acc;
+    }
   }
   if (Ks64 || Ks32)
     for (int t = KS_NNZ + threadIdx.x; t < KS_STRIDE; t += blockDim.x) {
@@ -309,16 +312,17 @@ __global__ void __launch_bounds__(STIFF_THREADS) k_stiffness(
   if (Ygrav)
     for (int t = threadIdx.x; t < NEDOF; t += blockDim.x) {
       int a = t / 3, d = t % 3;
-      Ygrav[(size_t)le * NEDOF + t] = (d == 2) ? -(swd[a] * gam[im]) : -0.0;
+      int ps = pos[(size_t)le * NGLL + a];
+      if (ps >= 0) Ygrav[(size_t)ps * 3 + d] = (d == 2) ? -(swd[a] * gam[im]) : -0.0;
     }
 }
 
 void launch_stiffness(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
                       const double* nu, const double* gam, double* Ks64, float* Ks32, double* Ydiag,
-                      double* Ygrav, const int* d_entry, cudaStream_t s) {
+                      double* Ygrav, const int* d_entry, const int* pos, cudaStream_t s) {
   if (nel <= 0) return;
   SG_LAUNCH k_stiffness<<<nel, STIFF_THREADS, 0, s>>>(geo, mat_id, elist, nel, ym, nu, gam, Ks64, Ks32, Ydiag, Ygrav,
-                                           d_entry);
+                                           d_entry, pos);
 }
 
 // Expand the sparse symmetric layout to the reference's dense column-major
@@ -356,7 +360,7 @@ void set_apply_variant(int v) { g_apply_variant = v; }
 __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_dense64(
     const double* __restrict__ K, const int* __restrict__ ge, int nelmt, const double* __restrict__ pold,
     const double* __restrict__ z, int combine, double* __restrict__ Y, const ColState* __restrict__ cs,
-    const PcgGlobal* __restrict__ G) {
+    const PcgGlobal* __restrict__ G, const int* __restrict__ pos) {
   if (G && G->all_done) return;
   const int lane = threadIdx.x & 31;
   const int w0 = blockIdx.x * APPLY_WARPS + (threadIdx.x >> 5);
@@ -381,10 +385,15 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_dense64(
       y1 = fma(__ldcs(col + lane + 32), pc, y1);
       if (lane < 17) y2 = fma(__ldcs(col + lane + 64), pc, y2);
     }
-    double* yo = Y + (size_t)e * NEDOF;
-    yo[lane] = y0;
-    yo[lane + 32] = y1;
-    if (lane < 17) yo[lane + 64] = y2;
+    // row r = 3a + d goes to the gather position of slot (e, a)
+    const int* pe = pos + (size_t)e * NGLL;
+    int q0 = pe[lane / 3], q1 = pe[(lane + 32) / 3];
+    if (q0 >= 0) Y[(size_t)q0 * 3 + lane % 3] = y0;
+    if (q1 >= 0) Y[(size_t)q1 * 3 + (lane + 32) % 3] = y1;
+    if (lane < 17) {
+      int q2 = pe[(lane + 64) / 3];
+      if (q2 >= 0) Y[(size_t)q2 * 3 + (lane + 64) % 3] = y2;
+    }
   }
 }
 
@@ -398,7 +407,7 @@ template <typename V, int KR>
 __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse(
     const V* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const V* __restrict__ pold,
     const V* __restrict__ z, int combine, V* __restrict__ Y, const ColState* __restrict__ cs,
-    const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g) {
+    const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g, const int* __restrict__ pos) {
   if (G && G->all_done) return;
   extern __shared__ __align__(128) unsigned char smem[];
   int* nbr = (int*)smem;                                   // 27*19 ints (2064 B incl. pad)
@@ -455,11 +464,14 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse(
           }
         }
       }
-      V* yo = Y + ((size_t)e * NEDOF + 3 * lane) * KR;
+      const int q = pos[(size_t)e * NGLL + lane];
+      if (q >= 0) {
+        V* yo = Y + (size_t)q * 3 * KR;
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
+        for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int j = 0; j < KR; ++j) yo[c * KR + j] = acc[c][j];
+          for (int j = 0; j < KR; ++j) yo[c * KR + j] = acc[c][j];
+      }
     }
     __syncwarp();
   }
@@ -506,7 +518,7 @@ template <typename V, int KR>
 __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
     const V* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const V* __restrict__ pold,
     const V* __restrict__ z, int combine, V* __restrict__ Y, const ColState* __restrict__ cs,
-    const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g) {
+    const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g, const int* __restrict__ pos) {
   if (G && G->all_done) return;
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int PST = (NEDOF * KR + 3) & ~3;
@@ -592,11 +604,14 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
           }
         }
       }
-      V* yo = Y + ((size_t)e * NEDOF + 3 * lane) * KR;
+      const int q = pos[(size_t)e * NGLL + lane];
+      if (q >= 0) {
+        V* yo = Y + (size_t)q * 3 * KR;
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
+        for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int j = 0; j < KR; ++j) yo[c * KR + j] = acc[c][j];
+          for (int j = 0; j < KR; ++j) yo[c * KR + j] = acc[c][j];
+      }
     }
     __syncwarp();
   }
@@ -623,12 +638,13 @@ static size_t apply_sparse_smem() {
 
 template <typename V, int KR>
 void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_old, const V* z, int combine, V* Y,
-               const ColState* cs, const PcgGlobal* G, const int* d_nbr, cudaStream_t s) {
+               const ColState* cs, const PcgGlobal* G, const int* d_nbr, const int* pos, cudaStream_t s) {
   if (nelmt <= 0) return;
   int blocks = (nelmt + APPLY_WARPS - 1) / APPLY_WARPS;
   if (dense) {
     if constexpr (std::is_same<V, double>::value && KR == 1)
-      SG_LAUNCH k_apply_dense64<<<blocks, APPLY_WARPS * 32, 0, s>>>((const double*)K, ge, nelmt, p_old, z, combine, Y, cs, G);
+      SG_LAUNCH k_apply_dense64<<<blocks, APPLY_WARPS * 32, 0, s>>>((const double*)K, ge, nelmt, p_old, z, combine, Y, cs, G,
+                                                                    pos);
     return;
   }
   if (g_apply_variant == 1) {
@@ -643,7 +659,7 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
     if (per_sm < 1) per_sm = 1;
     int grid = std::min(blocks, 152 * per_sm);
     SG_LAUNCH k_apply_sparse_tma<V, KR><<<grid, APPLY_WARPS * 32, sm, s>>>((const V*)K, ge, nelmt, p_old, z, combine, Y, cs,
-                                                                 G, d_nbr);
+                                                                 G, d_nbr, pos);
     return;
   }
   size_t sm = apply_sparse_smem<V, KR>();
@@ -653,7 +669,7 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
     attr = true;
   }
   SG_LAUNCH k_apply_sparse<V, KR><<<blocks, APPLY_WARPS * 32, sm, s>>>((const V*)K, ge, nelmt, p_old, z, combine, Y, cs, G,
-                                                               d_nbr);
+                                                               d_nbr, pos);
 }
 
 // ---------------------------------------------------------------------------
@@ -683,7 +699,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
       for (int j = 0; j < KR; ++j) acc[d][j] = (V)0;
     const int s1 = ptr[g + 1];
     for (int s = ptr[g]; s < s1; ++s) {
-      const V* y = Y + (size_t)ent[s] * 3 * KR;
+      const V* y = Y + (size_t)s * 3 * KR;   // producers wrote slot s at its gather position
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         V yv[KR];
@@ -766,7 +782,7 @@ __global__ void k_gather_plain(const int* __restrict__ ptr, const int* __restric
     acc[d] = (accumulate && gd) ? out[(size_t)gd * KR + j] : (V)0;
   }
   for (int s = ptr[g]; s < ptr[g + 1]; ++s) {
-    const V* y = Y + (size_t)ent[s] * 3 * KR;
+    const V* y = Y + (size_t)s * 3 * KR;
 #pragma unroll
     for (int d = 0; d < 3; ++d) acc[d] = acc[d] + y[d * KR + j];
   }
@@ -805,24 +821,51 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
   DotAcc<V> rza, rra;
   if (live) {
     const size_t n = (size_t)n1 * KR;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      const size_t row = i / KR;
-      V ri;
-      if (init) {
-        ri = f[i] - kp[i];
-      } else {
-        V pi = p[i];
-        V ui = fmav<V>(alpha, pi, u[i]);
-        u[i] = ui;
-        mpv = fmax(mpv, fabs(pi));
-        muv = fmax(muv, fabs(ui));
-        ri = fmav<V>(-alpha, kp[i], r[i]);
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (init) {
+      for (; i < n; i += stride) {
+        V ri = f[i] - kp[i];
+        V zi = dprecon[i / KR] * ri;
+        r[i] = ri;
+        z[i] = zi;
+        rza.add(ri, zi);
+        rra.add(ri, ri);
       }
-      V zi = dprecon[row] * ri;
-      r[i] = ri;
-      z[i] = zi;
-      rza.add(ri, zi);
-      rra.add(ri, ri);
+    } else {
+      // four independent rows per trip keep enough loads in flight
+      constexpr int U = 4;
+      for (; i + (U - 1) * stride < n; i += U * stride) {
+        V pi[U], ui[U], ri[U], ki[U], di[U];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+          const size_t o = i + q * stride;
+          pi[q] = p[o]; ui[q] = u[o]; ri[q] = r[o]; ki[q] = kp[o]; di[q] = dprecon[o / KR];
+        }
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+          const size_t o = i + q * stride;
+          V un = fmav<V>(alpha, pi[q], ui[q]);
+          V rn = fmav<V>(-alpha, ki[q], ri[q]);
+          V zn = di[q] * rn;
+          u[o] = un; r[o] = rn; z[o] = zn;
+          mpv = fmax(mpv, fabs(pi[q]));
+          muv = fmax(muv, fabs(un));
+          rza.add(rn, zn);
+          rra.add(rn, rn);
+        }
+      }
+      for (; i < n; i += stride) {
+        V pi = p[i];
+        V un = fmav<V>(alpha, pi, u[i]);
+        V rn = fmav<V>(-alpha, kp[i], r[i]);
+        V zn = dprecon[i / KR] * rn;
+        u[i] = un; r[i] = rn; z[i] = zn;
+        mpv = fmax(mpv, fabs(pi));
+        muv = fmax(muv, fabs(un));
+        rza.add(rn, zn);
+        rra.add(rn, rn);
+      }
     }
   }
   double mp = (double)mpv, mu = (double)muv, rz = rza.value(), rr = rra.value();
@@ -947,7 +990,7 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
     const double* __restrict__ geo, const int* __restrict__ elist, int nel, const int* __restrict__ ge,
     const int* __restrict__ mat_id, const double* __restrict__ x, int xstride, int xcol, const MatF* __restrict__ mf,
     double dt, int nl_isconv, int finalize, double* __restrict__ evpt, double* __restrict__ stress,
-    double* __restrict__ Yb, int ystride, int ycol, double* __restrict__ fmax_part) {
+    double* __restrict__ Yb, int ystride, int ycol, double* __restrict__ fmax_part, const int* __restrict__ pos) {
   __shared__ double s_eld[STRESS_WARPS][NEDOF];
   __shared__ double s_q[STRESS_WARPS][NGLL][9];
   __shared__ double s_fmax[STRESS_WARPS];
@@ -1105,8 +1148,11 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
           for (int c = 0; c < 3; ++c) F[c] = F[c] + s_q[warp][i][3 * c + a] * dl;
         }
       }
-      double* yo = Yb + ((size_t)le * NEDOF + 3 * n) * ystride + ycol;
-      yo[0] = F[0]; yo[ystride] = F[1]; yo[2 * ystride] = F[2];
+      const int q = pos[(size_t)le * NGLL + n];
+      if (q >= 0) {
+        double* yo = Yb + ((size_t)q * 3) * ystride + ycol;
+        yo[0] = F[0]; yo[ystride] = F[1]; yo[2 * ystride] = F[2];
+      }
     }
     __syncwarp();
   }
@@ -1125,11 +1171,11 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
 void launch_stress_update(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
                           const double* x, int xstride, int xcol, const MatF* mf, double dt, int nl_isconv,
                           int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
-                          double* fmax_part, cudaStream_t s) {
+                          double* fmax_part, const int* pos, cudaStream_t s) {
   // fixed grid so that fmax_part has NPART entries
   SG_LAUNCH k_stress_update<<<NPART, STRESS_WARPS * 32, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, xstride, xcol, mf, dt,
                                                        nl_isconv, finalize, evpt, stress, Yb, ystride, ycol,
-                                                       fmax_part);
+                                                       fmax_part, pos);
 }
 
 // elastic_stress (src/postprocess.f90:40-79): sigma = C B x per GLL point
@@ -1207,7 +1253,8 @@ void launch_overburden(const double* g_coord, const int* g_num, const int* mat_i
 // src/excavation_library.f90:186-236).  One thread per (element, node).
 __global__ void k_release_load(const double* __restrict__ geo, const int* __restrict__ elist, int nel,
                                const int* __restrict__ mat_id, const double* __restrict__ gam,
-                               const double* __restrict__ stress, double* __restrict__ Ye) {
+                               const double* __restrict__ stress, double* __restrict__ Ye,
+                               const int* __restrict__ pos) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nel * NGLL) return;
   int le = t / NGLL, n = t - le * NGLL;
@@ -1226,16 +1273,18 @@ __global__ void k_release_load(const double* __restrict__ geo, const int* __rest
   }
   const double* gn = geo + ((size_t)e * NGLL + n) * GEO_STRIDE;
   double eld = gn[9] * c_w[n];
-  double* yo = Ye + (size_t)le * NEDOF + 3 * n;
+  const int q = pos[(size_t)le * NGLL + n];
+  if (q < 0) return;
+  double* yo = Ye + (size_t)q * 3;
   yo[0] = F[0];
   yo[1] = F[1];
   yo[2] = eld * gam[mat_id[e] - 1] + F[2];
 }
 
 void launch_release_load(const double* geo, const int* elist, int nel, const int* mat_id, const double* gam,
-                         const double* stress, double* Ye, cudaStream_t s) {
+                         const double* stress, double* Ye, const int* pos, cudaStream_t s) {
   int n = nel * NGLL;
-  if (n > 0) SG_LAUNCH k_release_load<<<(n + 127) / 128, 128, 0, s>>>(geo, elist, nel, mat_id, gam, stress, Ye);
+  if (n > 0) SG_LAUNCH k_release_load<<<(n + 127) / 128, 128, 0, s>>>(geo, elist, nel, mat_id, gam, stress, Ye, pos);
 }
 
 // ---------------------------------------------------------------------------
@@ -1365,7 +1414,7 @@ void launch_invert_diag(int n1, double* dprecon, float* dprecon32, cudaStream_t 
 // explicit instantiations
 #define SG_INST(V, KR)                                                                                          \
   template void pcg_apply<V, KR>(int, const void*, const int*, int, const V*, const V*, int, V*, const ColState*, \
-                                 const PcgGlobal*, const int*, cudaStream_t);                                   \
+                                 const PcgGlobal*, const int*, const int*, cudaStream_t);                                   \
   template void pcg_gather<V, KR>(const GatherTopo&, const V*, V*, V*, const V*, int, ColState*, PcgGlobal*,    \
                                   double*, cudaStream_t);                                                       \
   template void pcg_update<V, KR>(int, V*, V*, V*, const V*, const V*, const V*, const V*, int, ColState*,      \

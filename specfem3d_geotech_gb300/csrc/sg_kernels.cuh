@@ -44,8 +44,10 @@ long long launch_count();        // kernel launches issued so far (host counter)
 void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline
 int apply_error_flag(cudaStream_t s);  // 1 if an apply kernel timed out on an mbarrier
 template <typename V, int KR>
+// Y receives element slot (e, a)'s three rows (x KR) at the slot's gather
+// position pos[e*27+a] (slots of fully fixed nodes, pos < 0, are skipped).
 void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_old, const V* z, int combine,
-               V* Y, const ColState* cs, const PcgGlobal* G, const int* d_nbr, cudaStream_t s);
+               V* Y, const ColState* cs, const PcgGlobal* G, const int* d_nbr, const int* pos, cudaStream_t s);
 template <typename V, int KR>
 void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mode, ColState* cs,
                 PcgGlobal* G, double* part, cudaStream_t s);
@@ -57,14 +59,14 @@ void pcg_update(int n1, V* u, V* r, V* z, const V* p, const V* kp, const V* f, c
 void launch_stress_update(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
                           const double* x, int xstride, int xcol, const MatF* mf, double dt, int nl_isconv,
                           int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
-                          double* fmax_part, cudaStream_t s);
+                          double* fmax_part, const int* pos, cudaStream_t s);
 void launch_elastic_stress(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
                            const double* x, int xstride, int xcol, const MatF* mf, int accumulate, double* stress,
                            cudaStream_t s);
 void launch_overburden(const double* g_coord, const int* g_num, const int* mat_id, const double* gam, int nelmt,
                        double z0, double p0, double k0, double* stress, cudaStream_t s);
 void launch_release_load(const double* geo, const int* elist, int nel, const int* mat_id, const double* gam,
-                         const double* stress, double* Ye, cudaStream_t s);
+                         const double* stress, double* Ye, const int* pos, cudaStream_t s);
 void launch_nl_check(int n1, int KR, int k, const double* x, double* oldx, double* part, cudaStream_t s);
 void launch_load_combine(int n1, int KR, const double* extload, const double* bodyload, double* load,
                          cudaStream_t s);

@@ -116,6 +116,12 @@ __global__ void k_topo_compact(const int* __restrict__ flag, const int* __restri
   if (k == 0) gptr[gid[n]] = ptr[n];
 }
 
+// gather position of every slot (its index in ent), -1 for slots of fully fixed nodes
+__global__ void k_topo_pos(const int* __restrict__ ent, int nent, int* __restrict__ pos) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nent) pos[ent[i]] = i;
+}
+
 // restore increasing element order inside each group (insertion sort)
 __global__ void k_topo_sort(const int* __restrict__ ptr, int n, int* __restrict__ ent) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -159,6 +165,7 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
   const size_t oFill = take(sizeof(int) * (n1 + 1)), oDof = take(sizeof(int) * 3 * (n1 + 1));
   const size_t oFlag = take(sizeof(int) * (n1 + 1)), oGid = take(sizeof(int) * (n1 + 1));
   const size_t oGptr = take(sizeof(int) * (n1 + 1)), oGdof = take(sizeof(int) * 3 * (n1 + 1));
+  const size_t oPos = take(sizeof(int) * nslots);
   if (off > SG_NOALLOC_SCRATCH_BYTES) {
     tag(errtag, "ERROR: problem needs " + std::to_string(off >> 20) +
                     " MiB of device scratch; sg_pcg_solve_noalloc is limited to 64 MiB (use sg_pcg_solve)!");
@@ -194,6 +201,7 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
   int *dPtr = (int*)(base + oPtr), *dFill = (int*)(base + oFill), *dDof = (int*)(base + oDof);
   int *dFlag = (int*)(base + oFlag), *dGid = (int*)(base + oGid), *dGptr = (int*)(base + oGptr);
   int* dGdof = (int*)(base + oGdof);
+  int* dPos = (int*)(base + oPos);
   cudaStream_t s = 0;
   cudaMemcpyAsync(dK, k, sizeof(double) * (size_t)nelmt * NEDOF * NEDOF, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(dGe, gdof_elmt, sizeof(int) * (size_t)nelmt * NEDOF, cudaMemcpyHostToDevice, s);
@@ -215,6 +223,10 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
   k_topo_flags<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(dCnt, (int)n1, dFlag);
   k_topo_scan<<<1, 1024, 0, s>>>(dFlag, (int)n1, dGid);
   k_topo_compact<<<(unsigned)((n1 + 255) / 256), 256, 0, s>>>(dFlag, dGid, dPtr, dDof, (int)n1, dGptr, dGdof);
+  cudaMemsetAsync(dPos, 0xff, sizeof(int) * nslots, s);  // -1 everywhere, then the occupied slots
+  int nent = 0;
+  cudaMemcpy(&nent, dPtr + n1, sizeof(int), cudaMemcpyDeviceToHost);
+  if (nent > 0) k_topo_pos<<<(unsigned)((nent + 255) / 256), 256, 0, s>>>(dEnt, nent, dPos);
   int ngroups = 0;
   if (cudaMemcpy(&ngroups, dGid + n1, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
     tag(errtag, std::string("ERROR: CUDA failure: ") + cudaGetErrorString(cudaGetLastError()));
@@ -226,6 +238,7 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
   T.d_ptr = dGptr;
   T.d_ent = dEnt;
   T.d_dof = dGdof;
+  T.d_pos = dPos;
   // PCG state: per-column scalars, control word, direction and product start at zero
   ColState hcs[16];
   std::memset(hcs, 0, sizeof(hcs));
@@ -240,7 +253,7 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
   cudaMemsetAsync(dP, 0, sizeof(double) * n1, s);
   cudaMemsetAsync(dKp, 0, sizeof(double) * n1, s);
   // kp = K u, r = f - kp, z = D r, p = z (src/solver.f90:38-50)
-  pcg_apply<double, 1>(1, dK, dGe, nelmt, dU, (const double*)nullptr, 0, dY, dCs, dG, nullptr, s);
+  pcg_apply<double, 1>(1, dK, dGe, nelmt, dU, (const double*)nullptr, 0, dY, dCs, dG, nullptr, dPos, s);
   pcg_gather<double, 1>(T, dY, dKp, dP, dZ, 0, dCs, dG, dPart, s);
   pcg_update<double, 1>((int)n1, dU, dR, dZ, dP, dKp, dF, dDp, 1, dCs, dG, dPart, s);
   const int chunk = 16;
@@ -248,7 +261,7 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
   PcgGlobal got;
   for (;;) {
     for (int c = 0; c < chunk; ++c) {
-      pcg_apply<double, 1>(1, dK, dGe, nelmt, dP, dZ, 1, dY, dCs, dG, nullptr, s);
+      pcg_apply<double, 1>(1, dK, dGe, nelmt, dP, dZ, 1, dY, dCs, dG, nullptr, dPos, s);
       pcg_gather<double, 1>(T, dY, dKp, dP, dZ, 1, dCs, dG, dPart, s);
       pcg_update<double, 1>((int)n1, dU, dR, dZ, dP, dKp, dF, dDp, 0, dCs, dG, dPart, s);
     }
