@@ -347,9 +347,14 @@ def run_ours(args, rank, world, local):
                        "pcg_iters_per_plastic_iter": n_cg_ref,
                        "mixed_batched_over_plain": rate_all / rate64 if rate64 == rate64 else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "kernel": f"k_apply_sparse_tma<float,{kr}>",
+                     "traffic": traffic, "kernel": ("k_apply_tc" if os.environ.get("SG_APPLY_VARIANT") == "2"
+                                                    else "k_apply_sparse_tma") + f"<float,{kr}>",
                      "algorithmic_bytes_per_launch": bytes_apply, "avg_launch_ms": apply_ms,
                      "peak_source": peak_kind},
+        "kernel_ms_per_pcg_iter": {"apply": apply_ms,
+                                   "gather": prof["gather_ms"] / max(1, prof["apply_launches"]),
+                                   "update": prof["update_ms"] / max(1, prof["apply_launches"]),
+                                   "stress_per_step": prof["stress_ms"] / max(1, args.steps)},
         "gpu_launches": prof["launches"],
         "clocks": clk,
         "e2e": e2e,

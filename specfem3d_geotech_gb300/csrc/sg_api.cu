@@ -294,6 +294,7 @@ sg_ctx* sg_create(int device, size_t hbm_budget) {
   c->d_entry = c->alloc<int>(KS_NNZ);
   cudaMemcpy(c->d_nbr, T.nbr, sizeof(T.nbr), cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_entry, T.entry, sizeof(T.entry), cudaMemcpyHostToDevice);
+  set_entry_table(c->d_entry);
   if (cudaGetLastError() != cudaSuccess) {
     g_create_status = SG_ERR_NODEVICE;
     delete c;
@@ -1080,7 +1081,10 @@ static int batch_iteration(sg_model* M) {
     S.res.failed = (S.res.nl_iter == ctl->nl_maxiter);
     slot_finish(M, t);
   }
-  if (apply_error_flag(s)) { c->err = "element apply: bulk-copy wait timed out"; return SG_ERR_TIMEOUT; }
+  if (apply_error_flag(s) || apply_tc_error_flag(s)) {
+    c->err = "element apply: a bounded wait timed out";
+    return SG_ERR_TIMEOUT;
+  }
   return c->check(cudaGetLastError(), "plastic iteration") ? SG_OK : SG_ERR_CUDA;
 }
 

@@ -146,6 +146,31 @@ __device__ __forceinline__ void loadv(const V* __restrict__ src, V (&out)[KR]) {
   }
 }
 
+
+// Store a node's 3 x KR results (one contiguous run) with 16-byte stores.
+template <typename V, int KR>
+__device__ __forceinline__ void storev3(V* __restrict__ dst, const V (&acc)[3][KR]) {
+  if constexpr (std::is_same<V, float>::value && KR % 4 == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int q = 0; q < KR / 4; ++q)
+        reinterpret_cast<float4*>(dst + c * KR)[q] =
+            make_float4(acc[c][4 * q], acc[c][4 * q + 1], acc[c][4 * q + 2], acc[c][4 * q + 3]);
+  } else if constexpr (std::is_same<V, double>::value && KR % 2 == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int q = 0; q < KR / 2; ++q)
+        reinterpret_cast<double2*>(dst + c * KR)[q] = make_double2(acc[c][2 * q], acc[c][2 * q + 1]);
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int j = 0; j < KR; ++j) dst[c * KR + j] = acc[c][j];
+  }
+}
+
 // last-block election: returns true in the block that finished last.
 __device__ __forceinline__ bool last_block(unsigned* counter) {
   __shared__ bool am_last;
@@ -353,6 +378,9 @@ constexpr int APPLY_WARPS = 4;
 // 0 = register-staged loads, 1 = TMA bulk-copy pipeline (default)
 int g_apply_variant = 1;
 void set_apply_variant(int v) { g_apply_variant = v; }
+// device copy of the stored-entry table, needed by the tensor-core apply
+const int* g_entry_dev = nullptr;
+void set_entry_table(const int* d_entry) { g_entry_dev = d_entry; }
 
 // Dense FP64 81x81, one right-hand side (the drop-in).  One warp per element,
 // lane l owns rows l, l+32, l+64; column c of K_e is 81 contiguous doubles,
@@ -465,13 +493,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse(
         }
       }
       const int q = pos[(size_t)e * NGLL + lane];
-      if (q >= 0) {
-        V* yo = Y + (size_t)q * 3 * KR;
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int j = 0; j < KR; ++j) yo[c * KR + j] = acc[c][j];
-      }
+      if (q >= 0) storev3<V, KR>(Y + (size_t)q * 3 * KR, acc);
     }
     __syncwarp();
   }
@@ -605,13 +627,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
         }
       }
       const int q = pos[(size_t)e * NGLL + lane];
-      if (q >= 0) {
-        V* yo = Y + (size_t)q * 3 * KR;
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int j = 0; j < KR; ++j) yo[c * KR + j] = acc[c][j];
-      }
+      if (q >= 0) storev3<V, KR>(Y + (size_t)q * 3 * KR, acc);
     }
     __syncwarp();
   }
@@ -647,7 +663,13 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
                                                                     pos);
     return;
   }
-  if (g_apply_variant == 1) {
+  if constexpr (std::is_same<V, float>::value && (KR == 8 || KR == 16)) {
+    if (g_apply_variant == 2) {
+      launch_apply_tc<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, g_entry_dev, pos, s);
+      return;
+    }
+  }
+  if (g_apply_variant >= 1) {
     size_t sm = apply_tma_smem<V, KR>();
     static bool attr = false;
     if (!attr) {

@@ -41,7 +41,13 @@ struct MatF {
 
 // Kernel launch wrappers (sg_kernels.cu)
 long long launch_count();        // kernel launches issued so far (host counter)
-void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline
+void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline, 2 tensor cores for 8/16 FP32 RHS
+void set_entry_table(const int* d_entry);
+int apply_tc_error_flag(cudaStream_t s);
+template <int KR>
+void launch_apply_tc(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
+                     float* Y, const ColState* cs, const PcgGlobal* G, const int* d_entry, const int* pos,
+                     cudaStream_t s);
 int apply_error_flag(cudaStream_t s);  // 1 if an apply kernel timed out on an mbarrier
 template <typename V, int KR>
 // Y receives element slot (e, a)'s three rows (x KR) at the slot's gather

@@ -265,3 +265,27 @@ def test_fos_mixed_batched_matches_oracle_critical_srf(ctx):
     fos, ntrials, nrounds = m.fos(sg.make_control(precision=sg.PREC_MIXED), lo=1.0, hi=2.0, step=0.05, k=8)
     assert abs(fos - 1.35) < 1e-12
     assert nrounds <= 3
+
+
+def test_tensor_core_apply_matches_simt(ctx, tmp_path):
+    """The tcgen05 batched apply (3xTF32, TMEM accumulators) reproduces the SIMT
+    FP32 apply's trials to the mixed-precision tolerance, 8 trials per batch."""
+    import subprocess
+    import sys
+    srfs = [1.0, 1.02, 1.05, 1.1, 1.15, 1.2, 1.25, 1.3]
+    mesh = meshgen.slope2d()
+    m = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    ctl = sg.make_control(precision=sg.PREC_MIXED)
+    res1, x1 = m.trials(srfs, ctl, want_x=True)
+    out = tmp_path / "tc.npz"
+    code = ("import sys; sys.path.insert(0, %r); import numpy as np; import specfem3d_geotech_gb300 as sg;"
+            "from specfem3d_geotech_gb300 import meshgen; m = sg.Model(meshgen.slope2d(), precision=sg.PREC_MIXED);"
+            "r, x = m.trials(%r, sg.make_control(precision=sg.PREC_MIXED), want_x=True);"
+            "np.savez(%r, x=x, nl=np.array([t['nl_iter'] for t in r]))") % (
+        os.path.dirname(os.path.dirname(os.path.abspath(__file__))), srfs, str(out))
+    env = dict(os.environ, SG_APPLY_VARIANT="2")
+    subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=600)
+    d = np.load(out)
+    assert [r["nl_iter"] for r in res1] == d["nl"].tolist()
+    for t in range(len(srfs)):
+        assert rel(d["x"][t], x1[t]) <= MIXED_TOL
