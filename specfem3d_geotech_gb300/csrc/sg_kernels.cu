@@ -699,12 +699,31 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
 // mode 0: plain (kp only); mode 1: PCG iteration -- also p = z + beta*p for
 // the node's dofs and the p.kp partial; the last block forms alpha = rz/p.kp.
 // ---------------------------------------------------------------------------
+// Each warp takes 32 consecutive groups; their element slots are one
+// contiguous run of Y (the producers wrote slot s at position s), which the
+// warp copies into shared memory with coalesced 16-byte loads before each lane
+// sums its own group's slots in order.  A run longer than the buffer is read
+// directly from global memory.
+constexpr int GATHER_WARPS = RED_THREADS / 32;
+
+template <typename V, int KR>
+struct GatherBuf {
+  static constexpr int ROW = 3 * KR;                                    // values per slot
+  // slots per warp buffer: 32 groups hold ~108 slots on average (27/8 per node)
+  static constexpr int CAP_BYTES = (20480 / (ROW * (int)sizeof(V))) & ~1;
+  static constexpr int CAP = CAP_BYTES < 192 ? CAP_BYTES : 192;
+  static constexpr size_t SMEM = (size_t)GATHER_WARPS * CAP * ROW * sizeof(V);
+};
+
 template <typename V, int KR>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
     const int* __restrict__ ptr, const int* __restrict__ ent, const int* __restrict__ dof, int ng,
     const V* __restrict__ Y, V* __restrict__ kp, V* __restrict__ p, const V* __restrict__ z, int mode,
     ColState* __restrict__ cs, PcgGlobal* __restrict__ G, double* __restrict__ part) {
   if (G->all_done) return;
+  constexpr int ROW = GatherBuf<V, KR>::ROW, CAP = GatherBuf<V, KR>::CAP;
+  extern __shared__ __align__(128) unsigned char gsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   DotAcc<V> dacc[KR];
   bool live[KR];
   V beta[KR];
@@ -713,44 +732,58 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
     live[j] = cs[j].active && !cs[j].done;
     beta[j] = (V)cs[j].beta;
   }
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
-    V acc[3][KR];
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int j = 0; j < KR; ++j) acc[d][j] = (V)0;
-    const int s1 = ptr[g + 1];
-    for (int s = ptr[g]; s < s1; ++s) {
-      const V* y = Y + (size_t)s * 3 * KR;   // producers wrote slot s at its gather position
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        V yv[KR];
-        loadv<V, KR>(y + d * KR, yv);
-#pragma unroll
-        for (int j = 0; j < KR; ++j) acc[d][j] = acc[d][j] + yv[j];
+  V* buf = reinterpret_cast<V*>(gsm) + (size_t)warp * CAP * ROW;
+  for (int g0 = (blockIdx.x * GATHER_WARPS + warp) * 32; g0 < ng; g0 += gridDim.x * GATHER_WARPS * 32) {
+    const int g = g0 + lane;
+    const int gend = min(g0 + 32, ng);
+    const int s0 = ptr[g0], s1 = ptr[gend];
+    const int a = g < ng ? ptr[g] : s1, b = g < ng ? ptr[g + 1] : s1;
+    const bool staged = (s1 - s0) <= CAP;
+    if (staged) {
+      const size_t base = (size_t)s0 * ROW;
+      const int nval = (s1 - s0) * ROW;
+      if constexpr ((ROW * sizeof(V)) % 16 == 0) {
+        const float4* src = reinterpret_cast<const float4*>(Y + base);
+        float4* dst = reinterpret_cast<float4*>(buf);
+        const int n4 = nval * (int)sizeof(V) / 16;
+        for (int q = lane; q < n4; q += 32) dst[q] = __ldcs(src + q);
+      } else {
+        for (int q = lane; q < nval; q += 32) buf[q] = Y[base + q];
       }
     }
-#pragma unroll
+    __syncwarp();
+    // one dof of the node at a time keeps the accumulators to KR registers
+#pragma unroll 1
     for (int d = 0; d < 3; ++d) {
-      int gd = dof[3 * g + d];
+      V acc[KR];
+#pragma unroll
+      for (int j = 0; j < KR; ++j) acc[j] = (V)0;
+      for (int s = a; s < b; ++s) {
+        const V* y = (staged ? buf + (size_t)(s - s0) * ROW : Y + (size_t)s * ROW) + d * KR;
+        V yv[KR];
+        loadv<V, KR>(y, yv);
+#pragma unroll
+        for (int j = 0; j < KR; ++j) acc[j] = acc[j] + yv[j];
+      }
+      const int gd = g < ng ? dof[3 * g + d] : 0;
       if (!gd) continue;
 #pragma unroll
       for (int j = 0; j < KR; ++j) {
         size_t o = (size_t)gd * KR + j;
         if (mode == 0) {
-          kp[o] = acc[d][j];
+          kp[o] = acc[j];
         } else if (live[j]) {
           V pn = pdir(beta[j], p[o], z[o]);
           p[o] = pn;
-          kp[o] = acc[d][j];
-          dacc[j].add(pn, acc[d][j]);
+          kp[o] = acc[j];
+          dacc[j].add(pn, acc[j]);
         }
       }
     }
+    __syncwarp();
   }
   if (mode == 0) return;
   __shared__ double sred[RED_THREADS / 32][KR];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
   for (int j = 0; j < KR; ++j) {
     double v = dacc[j].value();
@@ -784,8 +817,14 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
 template <typename V, int KR>
 void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mode, ColState* cs, PcgGlobal* G,
                 double* part, cudaStream_t s) {
-  SG_LAUNCH k_pcg_gather<V, KR><<<NPART, RED_THREADS, 0, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, Y, kp, p, z, mode, cs,
-                                                     G, part);
+  constexpr size_t sm = GatherBuf<V, KR>::SMEM;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_pcg_gather<V, KR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  SG_LAUNCH k_pcg_gather<V, KR><<<NPART, RED_THREADS, sm, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, Y, kp, p, z, mode,
+                                                              cs, G, part);
 }
 
 // Plain gather without PCG state: out = (accumulate ? out : 0) + sum Y.
