@@ -147,6 +147,23 @@ __device__ __forceinline__ void loadv(const V* __restrict__ src, V (&out)[KR]) {
 }
 
 
+
+// Store KR consecutive values (16-byte vector stores when the row allows it).
+template <typename V, int KR>
+__device__ __forceinline__ void storev(V* __restrict__ dst, const V (&v)[KR]) {
+  if constexpr (std::is_same<V, float>::value && KR % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < KR / 4; ++q)
+      reinterpret_cast<float4*>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+  } else if constexpr (std::is_same<V, double>::value && KR % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < KR / 2; ++q) reinterpret_cast<double2*>(dst)[q] = make_double2(v[2 * q], v[2 * q + 1]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < KR; ++j) dst[j] = v[j];
+  }
+}
+
 // Store a node's 3 x KR results (one contiguous run) with 16-byte stores.
 template <typename V, int KR>
 __device__ __forceinline__ void storev3(V* __restrict__ dst, const V (&acc)[3][KR]) {
@@ -767,18 +784,23 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
       }
       const int gd = g < ng ? dof[3 * g + d] : 0;
       if (!gd) continue;
+      V* kpo = kp + (size_t)gd * KR;
+      if (mode == 0) {
+        storev<V, KR>(kpo, acc);
+        continue;
+      }
+      V pv[KR], zv[KR];
+      loadv<V, KR>(p + (size_t)gd * KR, pv);
+      loadv<V, KR>(z + (size_t)gd * KR, zv);
 #pragma unroll
       for (int j = 0; j < KR; ++j) {
-        size_t o = (size_t)gd * KR + j;
-        if (mode == 0) {
-          kp[o] = acc[j];
-        } else if (live[j]) {
-          V pn = pdir(beta[j], p[o], z[o]);
-          p[o] = pn;
-          kp[o] = acc[j];
-          dacc[j].add(pn, acc[j]);
+        if (live[j]) {
+          pv[j] = pdir(beta[j], pv[j], zv[j]);
+          dacc[j].add(pv[j], acc[j]);
         }
       }
+      storev<V, KR>(p + (size_t)gd * KR, pv);
+      storev<V, KR>(kpo, acc);
     }
     __syncwarp();
   }
