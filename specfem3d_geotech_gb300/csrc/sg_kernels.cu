@@ -563,15 +563,20 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
   constexpr int PST = (NEDOF * KR + 3) & ~3;
   constexpr int WSTRIDE = 2 * KS_STRIDE + PST;     // two K stages + the p tile
   constexpr unsigned KBYTES = KS_STRIDE * sizeof(V);
-  int* nbr = (int*)smem;                           // 27*19 ints
-  uint64_t* bars = (uint64_t*)(smem + 2064);       // 2 mbarriers per warp
-  V* wbase = (V*)(smem + 2064 + 16 * APPLY_WARPS + 48);  // 128-byte aligned base (2064+64+48 = 2176)
+  int* tab = (int*)smem;                           // 27*27 ints: block of (n,m) or -1
+  uint64_t* bars = (uint64_t*)(smem + 2944);       // 2 mbarriers per warp
+  V* wbase = (V*)(smem + 3072);                    // 128-byte aligned base
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   V* kbuf0 = wbase + (size_t)warp * WSTRIDE;
   V* kbuf1 = kbuf0 + KS_STRIDE;
   V* ps = kbuf1 + KS_STRIDE;
   uint64_t* bar = bars + 2 * warp;
-  for (int t = threadIdx.x; t < NGLL * KS_NBR; t += blockDim.x) nbr[t] = nbr_g[t];
+  for (int t = threadIdx.x; t < NGLL * NGLL; t += blockDim.x) tab[t] = -1;
+  __syncthreads();
+  for (int t = threadIdx.x; t < NGLL * KS_NBR; t += blockDim.x) {
+    const int n = t / KS_NBR, pk = nbr_g[t];
+    tab[n * NGLL + (pk & 31)] = ((pk >> 8) << 2) | ((pk >> 5) & 3);
+  }
   if (lane == 0) {
     mbar_init(bar, 1);
     mbar_init(bar + 1, 1);
@@ -623,23 +628,29 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
       for (int c = 0; c < 3; ++c)
 #pragma unroll
         for (int j = 0; j < KR; ++j) acc[c][j] = (V)0;
-      const int* tb = nbr + lane * KS_NBR;
-#pragma unroll
-      for (int s = 0; s < KS_NBR; ++s) {
-        int pk = tb[s];
-        int m = pk & 31, kind = (pk >> 5) & 3, off = pk >> 8;
-        int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
-        const V* kb = kcur + off;
+      // Source-node order: at step m every lane reads the same p_m rows (a
+      // shared-memory broadcast) and, if node m is coupled to its own node,
+      // its 3x3 block; each output still sums over m in increasing order.
+      const int* tb = tab + lane * NGLL;
+#pragma unroll 3
+      for (int m = 0; m < NGLL; ++m) {
         const V* pm = ps + 3 * m * KR;
+        V pv[3][KR];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          V pv[KR];
-          loadv<V, KR>(pm + d * KR, pv);
+        for (int d = 0; d < 3; ++d) loadv<V, KR>(pm + d * KR, pv[d]);
+        const int pk = tb[m];
+        if (pk >= 0) {
+          const int kind = pk & 3, off = pk >> 2;
+          const int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
+          const V* kb = kcur + off;
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            V kv = kb[c * sc + d * sd];
+          for (int d = 0; d < 3; ++d) {
 #pragma unroll
-            for (int j = 0; j < KR; ++j) acc[c][j] = fmav<V>(kv, pv[j], acc[c][j]);
+            for (int c = 0; c < 3; ++c) {
+              V kv = kb[c * sc + d * sd];
+#pragma unroll
+              for (int j = 0; j < KR; ++j) acc[c][j] = fmav<V>(kv, pv[d][j], acc[c][j]);
+            }
           }
         }
       }
@@ -654,7 +665,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
 
 template <typename V, int KR>
 static size_t apply_tma_smem() {
-  return 2176 + (size_t)APPLY_WARPS * (2 * KS_STRIDE + ((NEDOF * KR + 3) & ~3)) * sizeof(V);
+  return 3072 + (size_t)APPLY_WARPS * (2 * KS_STRIDE + ((NEDOF * KR + 3) & ~3)) * sizeof(V);
 }
 
 int apply_error_flag(cudaStream_t s) {
@@ -728,7 +739,7 @@ struct GatherBuf {
   static constexpr int ROW = 3 * KR;                                    // values per slot
   // slots per warp buffer: 32 groups hold ~108 slots on average (27/8 per node)
   static constexpr int CAP_BYTES = (20480 / (ROW * (int)sizeof(V))) & ~1;
-  static constexpr int CAP = CAP_BYTES < 192 ? CAP_BYTES : 192;
+  static constexpr int CAP = CAP_BYTES < 128 ? CAP_BYTES : 128;
   static constexpr size_t SMEM = (size_t)GATHER_WARPS * CAP * ROW * sizeof(V);
 };
 
