@@ -563,7 +563,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
   constexpr int PST = (NEDOF * KR + 3) & ~3;
   constexpr int WSTRIDE = 2 * KS_STRIDE + PST;     // two K stages + the p tile
   constexpr unsigned KBYTES = KS_STRIDE * sizeof(V);
-  int* tab = (int*)smem;                           // 27*27 ints: block of (n,m) or -1
+  int* nbr = (int*)smem;                           // 27*19 ints
   uint64_t* bars = (uint64_t*)(smem + 2944);       // 2 mbarriers per warp
   V* wbase = (V*)(smem + 3072);                    // 128-byte aligned base
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -571,12 +571,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
   V* kbuf1 = kbuf0 + KS_STRIDE;
   V* ps = kbuf1 + KS_STRIDE;
   uint64_t* bar = bars + 2 * warp;
-  for (int t = threadIdx.x; t < NGLL * NGLL; t += blockDim.x) tab[t] = -1;
-  __syncthreads();
-  for (int t = threadIdx.x; t < NGLL * KS_NBR; t += blockDim.x) {
-    const int n = t / KS_NBR, pk = nbr_g[t];
-    tab[n * NGLL + (pk & 31)] = ((pk >> 8) << 2) | ((pk >> 5) & 3);
-  }
+  for (int t = threadIdx.x; t < NGLL * KS_NBR; t += blockDim.x) nbr[t] = nbr_g[t];
   if (lane == 0) {
     mbar_init(bar, 1);
     mbar_init(bar + 1, 1);
@@ -628,28 +623,60 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
       for (int c = 0; c < 3; ++c)
 #pragma unroll
         for (int j = 0; j < KR; ++j) acc[c][j] = (V)0;
-      // Source-node order: at step m every lane reads the same p_m rows (a
-      // shared-memory broadcast) and, if node m is coupled to its own node,
-      // its 3x3 block; each output still sums over m in increasing order.
-      const int* tb = tab + lane * NGLL;
-#pragma unroll 3
-      for (int m = 0; m < NGLL; ++m) {
-        const V* pm = ps + 3 * m * KR;
-        V pv[3][KR];
+      const int* tb = nbr + lane * KS_NBR;
+      if constexpr (std::is_same<V, float>::value && KR % 2 == 0) {
+        // packed FP32x2 FMAs: two right-hand sides per instruction
+        float2 acc2[3][KR / 2];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) loadv<V, KR>(pm + d * KR, pv[d]);
-        const int pk = tb[m];
-        if (pk >= 0) {
-          const int kind = pk & 3, off = pk >> 2;
-          const int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int q = 0; q < KR / 2; ++q) acc2[c][q] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int s = 0; s < KS_NBR; ++s) {
+          int pk = tb[s];
+          int m = pk & 31, kind = (pk >> 5) & 3, off = pk >> 8;
+          int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
           const V* kb = kcur + off;
+          const V* pm = ps + 3 * m * KR;
 #pragma unroll
           for (int d = 0; d < 3; ++d) {
+            float2 pv2[KR / 2];
+#pragma unroll
+            for (int q = 0; q < KR / 4; ++q) {
+              float4 t = reinterpret_cast<const float4*>(pm + d * KR)[q];
+              pv2[2 * q] = make_float2(t.x, t.y);
+              pv2[2 * q + 1] = make_float2(t.z, t.w);
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const float kv = kb[c * sc + d * sd];
+              const float2 kk = make_float2(kv, kv);
+#pragma unroll
+              for (int q = 0; q < KR / 2; ++q) acc2[c][q] = __ffma2_rn(kk, pv2[q], acc2[c][q]);
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int q = 0; q < KR / 2; ++q) { acc[c][2 * q] = acc2[c][q].x; acc[c][2 * q + 1] = acc2[c][q].y; }
+      } else {
+#pragma unroll
+        for (int s = 0; s < KS_NBR; ++s) {
+          int pk = tb[s];
+          int m = pk & 31, kind = (pk >> 5) & 3, off = pk >> 8;
+          int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
+          const V* kb = kcur + off;
+          const V* pm = ps + 3 * m * KR;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            V pv[KR];
+            loadv<V, KR>(pm + d * KR, pv);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               V kv = kb[c * sc + d * sd];
 #pragma unroll
-              for (int j = 0; j < KR; ++j) acc[c][j] = fmav<V>(kv, pv[d][j], acc[c][j]);
+              for (int j = 0; j < KR; ++j) acc[c][j] = fmav<V>(kv, pv[j], acc[c][j]);
             }
           }
         }
