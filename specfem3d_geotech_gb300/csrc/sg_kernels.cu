@@ -560,7 +560,10 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
     const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g, const int* __restrict__ pos) {
   if (G && G->all_done) return;
   extern __shared__ __align__(128) unsigned char smem[];
-  constexpr int PST = (NEDOF * KR + 3) & ~3;
+  // p tile: one row of 3*KR values per node, padded so that node rows start
+  // 4 banks apart modulo 32 (a period-8 bank pattern for the 16-byte reads)
+  constexpr int PROW = 3 * KR + (KR >= 8 ? 4 : 0);
+  constexpr int PST = (NGLL * PROW + 3) & ~3;
   constexpr int WSTRIDE = 2 * KS_STRIDE + PST;     // two K stages + the p tile
   constexpr unsigned KBYTES = KS_STRIDE * sizeof(V);
   int* nbr = (int*)smem;                           // 27*19 ints
@@ -607,7 +610,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
           for (int j = 0; j < KR; ++j) pv[j] = pdir(beta[j], pv[j], zv[j]);
         }
 #pragma unroll
-        for (int j = 0; j < KR; ++j) ps[(3 * lane + d) * KR + j] = pv[j];
+        for (int j = 0; j < KR; ++j) ps[lane * PROW + d * KR + j] = pv[j];
       }
     }
     bool ok = mbar_wait(bar + (i & 1), (unsigned)((i >> 1) & 1));
@@ -637,7 +640,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
           int m = pk & 31, kind = (pk >> 5) & 3, off = pk >> 8;
           int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
           const V* kb = kcur + off;
-          const V* pm = ps + 3 * m * KR;
+          const V* pm = ps + m * PROW;
 #pragma unroll
           for (int d = 0; d < 3; ++d) {
             float2 pv2[KR / 2];
@@ -667,7 +670,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
           int m = pk & 31, kind = (pk >> 5) & 3, off = pk >> 8;
           int sc = (kind == 2) ? 1 : 3, sd = (kind == 2) ? 3 : 1;
           const V* kb = kcur + off;
-          const V* pm = ps + 3 * m * KR;
+          const V* pm = ps + m * PROW;
 #pragma unroll
           for (int d = 0; d < 3; ++d) {
             V pv[KR];
@@ -692,7 +695,8 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
 
 template <typename V, int KR>
 static size_t apply_tma_smem() {
-  return 3072 + (size_t)APPLY_WARPS * (2 * KS_STRIDE + ((NEDOF * KR + 3) & ~3)) * sizeof(V);
+  constexpr int PROW = 3 * KR + (KR >= 8 ? 4 : 0);
+  return 3072 + (size_t)APPLY_WARPS * (2 * KS_STRIDE + ((NGLL * PROW + 3) & ~3)) * sizeof(V);
 }
 
 int apply_error_flag(cudaStream_t s) {
