@@ -3,9 +3,8 @@
 //
 // Who needs it: hosts that own the GPU's memory themselves and forbid other
 // code from calling cudaMalloc -- for example a Fortran or C++ application
-// that runs under a fixed memory pool or a sub-allocator, a code path that is
-// later captured into a CUDA graph, or a library loaded into a process whose
-// allocator must not be bypassed.  sg_pcg_solve needs a context (sg_create),
+// that runs under a fixed memory pool or a sub-allocator, or a library loaded
+// into a process whose allocator must not be bypassed.  sg_pcg_solve needs a context (sg_create),
 // and the context allocates; this entry point needs neither.
 //
 // How: all device memory the solve uses -- the copies of the caller's
