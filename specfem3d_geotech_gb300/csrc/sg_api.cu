@@ -1081,7 +1081,7 @@ static int batch_iteration(sg_model* M) {
     S.res.failed = (S.res.nl_iter == ctl->nl_maxiter);
     slot_finish(M, t);
   }
-  if (apply_error_flag(s) || apply_tc_error_flag(s)) {
+  if (apply_error_flag(s) || apply_tc_error_flag(s) || apply_lanes_error_flag(s)) {
     c->err = "element apply: a bounded wait timed out";
     return SG_ERR_TIMEOUT;
   }

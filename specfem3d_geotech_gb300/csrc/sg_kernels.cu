@@ -724,7 +724,11 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
   }
   if constexpr (std::is_same<V, float>::value && (KR == 8 || KR == 16)) {
     if (g_apply_variant == 2) {
-      launch_apply_tc<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, g_entry_dev, pos, s);
+      SG_LAUNCH launch_apply_tc<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, g_entry_dev, pos, s);
+      return;
+    }
+    if (g_apply_variant == 3) {
+      SG_LAUNCH launch_apply_lanes<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, pos, s);
       return;
     }
   }

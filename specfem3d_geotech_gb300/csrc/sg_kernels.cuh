@@ -41,7 +41,8 @@ struct MatF {
 
 // Kernel launch wrappers (sg_kernels.cu)
 long long launch_count();        // kernel launches issued so far (host counter)
-void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline, 2 tensor cores for 8/16 FP32 RHS
+void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline, 2 tensor cores for 8/16 FP32 RHS,
+                                 // 3 lane per (element, RHS) for 8/16 FP32 RHS
 void set_entry_table(const int* d_entry);
 int apply_tc_error_flag(cudaStream_t s);
 template <int KR>
@@ -49,6 +50,10 @@ void launch_apply_tc(const float* Ks, const int* ge, int nelmt, const float* pol
                      float* Y, const ColState* cs, const PcgGlobal* G, const int* d_entry, const int* pos,
                      cudaStream_t s);
 int apply_error_flag(cudaStream_t s);  // 1 if an apply kernel timed out on an mbarrier
+template <int KR>
+void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
+                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, cudaStream_t s);
+int apply_lanes_error_flag(cudaStream_t s);
 template <typename V, int KR>
 // Y receives element slot (e, a)'s three rows (x KR) at the slot's gather
 // position pos[e*27+a] (slots of fully fixed nodes, pos < 0, are skipped).

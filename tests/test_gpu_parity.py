@@ -289,3 +289,32 @@ def test_tensor_core_apply_matches_simt(ctx, tmp_path):
     assert [r["nl_iter"] for r in res1] == d["nl"].tolist()
     for t in range(len(srfs)):
         assert rel(d["x"][t], x1[t]) <= MIXED_TOL
+
+
+def _variant_trials(variant, srfs, out):
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, %r); import numpy as np; import specfem3d_geotech_gb300 as sg;"
+            "from specfem3d_geotech_gb300 import meshgen; m = sg.Model(meshgen.slope2d(), precision=sg.PREC_MIXED);"
+            "r, x = m.trials(%r, sg.make_control(precision=sg.PREC_MIXED), want_x=True);"
+            "np.savez(%r, x=x, nl=np.array([t['nl_iter'] for t in r]), cg=np.array([t['cg_tot'] for t in r]))") % (
+        os.path.dirname(os.path.dirname(os.path.abspath(__file__))), srfs, str(out))
+    env = dict(os.environ, SG_APPLY_VARIANT=str(variant))
+    subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=600)
+    return np.load(out)
+
+
+@pytest.mark.parametrize("k", [8, 16])
+def test_lane_apply_matches_node_lane_apply(tmp_path, k):
+    """The lane-per-(element, trial) FP32 apply (sums in storage order) gives
+    the node-lane TMA apply's trials to the mixed-precision tolerance, with the
+    same plastic-iteration counts, for 8 and 16 trials per batch; two runs of
+    it are bitwise equal."""
+    srfs = [1.0 + 0.02 * t for t in range(k)]
+    a = _variant_trials(1, srfs, tmp_path / "v1.npz")
+    b = _variant_trials(3, srfs, tmp_path / "v3.npz")
+    c = _variant_trials(3, srfs, tmp_path / "v3b.npz")
+    assert a["nl"].tolist() == b["nl"].tolist()
+    for t in range(k):
+        assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
+    assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
