@@ -43,6 +43,7 @@ FOS_TRIALS = 8               # bisection trials per FOS solve on [1,3] to 0.01
 FOS_WORK = FOS_TRIALS * NL_MAXITER   # trial plastic iterations per FOS solve (upper bound)
 N_CG_REF = 825               # PCG iterations per plastic iteration of the FP64 reference algorithm on this mesh
 K_TRIALS = 8
+CPU_SAMPLE_ITERS = 200       # PCG iterations of the oracle's timed sample (about 10 s of CPU work)
 
 
 def peaks():
@@ -219,6 +220,15 @@ def run_reference(args, rank, world):
     return 0
 
 
+def apply_kernel_name(kr: int) -> str:
+    v = os.environ.get("SG_APPLY_VARIANT", "3")
+    if v == "2" and kr in (8, 16):
+        return f"k_apply_tc<{kr}>"
+    if v == "3" and kr in (8, 16):
+        return f"k_apply_lanes<{kr}>"
+    return f"k_apply_sparse_tma<float,{kr}>"
+
+
 def plain_fp64(sg, ctx, mesh, srf0, args):
     """Plain FP64 one-at-a-time trial on the same mesh: trial plastic iterations/s
     and PCG iterations per plastic iteration of the reference algorithm."""
@@ -347,8 +357,7 @@ def run_ours(args, rank, world, local):
                        "pcg_iters_per_plastic_iter": n_cg_ref,
                        "mixed_batched_over_plain": rate_all / rate64 if rate64 == rate64 else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "kernel": ("k_apply_tc" if os.environ.get("SG_APPLY_VARIANT") == "2"
-                                                    else "k_apply_sparse_tma") + f"<float,{kr}>",
+                     "traffic": traffic, "kernel": apply_kernel_name(kr),
                      "algorithmic_bytes_per_launch": bytes_apply, "avg_launch_ms": apply_ms,
                      "peak_source": peak_kind},
         "kernel_ms_per_pcg_iter": {"apply": apply_ms,
@@ -361,11 +370,12 @@ def run_ours(args, rank, world, local):
     }
     if rank == 0 and not args.no_cpu:
         t0 = time.time()
-        r = oracle_sample(n_cg=n_cg_ref)
+        r = oracle_sample(n_cg=n_cg_ref, iters=CPU_SAMPLE_ITERS)
         cpu_rate = 1.0 / r["t_plastic_iter_full"]
         line["cpu_baseline"] = {
             "value": cpu_rate / FOS_WORK, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": (f"oracle on a 6,000-element cut of the same slope (30 PCG iterations + 1 stress pass, "
+            "sample": (f"oracle on a 6,000-element cut of the same slope ({CPU_SAMPLE_ITERS} PCG iterations + "
+                       f"1 stress pass, "
                        f"{time.time() - t0:.0f} s), scaled by element count to 192k elements and to "
                        f"{n_cg_ref:.0f} PCG iterations per plastic iteration")}
     if rank == 0:

@@ -286,8 +286,8 @@ sg_ctx* sg_create(int device, size_t hbm_budget) {
   }
   cudaMallocHost((void**)&c->pin, 4096);
   upload_constants();
-  // SG_APPLY_VARIANT=0 selects the register-staged element apply instead of
-  // the TMA pipeline (kept for cross-checking the two).
+  // SG_APPLY_VARIANT selects another element apply for cross-checking:
+  // 0 register-staged, 1 TMA node lanes, 2 tensor cores (default 3).
   if (const char* v = std::getenv("SG_APPLY_VARIANT")) set_apply_variant(std::atoi(v));
   const KsTables& T = ks_tables();
   c->d_nbr = c->alloc<int>(NGLL * KS_NBR);

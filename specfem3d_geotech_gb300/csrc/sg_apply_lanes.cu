@@ -15,7 +15,9 @@
 // stage holds one 976-byte chunk (61 float4) of each of the warp's elements,
 // copied by cp.async.bulk with completion on the stage's mbarrier.  Lane 0
 // keeps NSTAGE-1 chunks in flight.  Chunk slots are 976 B apart, so the EPW
-// element slots of a stage fall on distinct 16-byte bank groups.  Every wait
+// element slots of a stage fall on distinct 16-byte bank groups.  The next
+// group's dof numbers and gather positions travel to shared memory by
+// cp.async while the current group computes.  Every wait
 // is bounded; a timeout sets a device flag, the warp drains its own copies
 // (bounded) and stops.
 //
@@ -130,14 +132,41 @@ __device__ __forceinline__ void for_chunks(F& f, std::integer_sequence<int, Cs..
 
 constexpr unsigned chunk_bytes(int c) { return (unsigned)(c == NCH - 1 ? LAST_F4 * 16 : CHF * 4); }
 
+constexpr int IDX = NEDOF + NGLL;  // per element: 81 dof numbers + 27 gather positions
+
 template <int KR>
 struct Shape {
   static constexpr int EPW = 32 / KR;                       // elements per warp
   static constexpr int STAGE_F = EPW * CHF;                 // floats per stage
   static constexpr int RING_F = NSTAGE * STAGE_F;           // floats per warp ring
+  static constexpr int IBUF = 2 * EPW * IDX;                // ints per warp: two groups of indices
   static constexpr int BAR_BYTES = 512;                     // NW * NSTAGE mbarriers, padded
-  static constexpr size_t SMEM = BAR_BYTES + (size_t)NW * RING_F * 4;
+  static constexpr size_t SMEM = BAR_BYTES + (size_t)NW * RING_F * 4 + (size_t)NW * IBUF * 4;
 };
+
+__device__ __forceinline__ void cp_async4(int* dst, const int* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// The warp copies group g's dof numbers and gather positions into buf
+// (4-byte cp.async, no registers held while they travel).
+template <int KR>
+__device__ __forceinline__ void prefetch_indices(const int* __restrict__ ge, const int* __restrict__ pos, int nelmt,
+                                                 int ngroups, int g, int* buf, int lane) {
+  using S = Shape<KR>;
+  if (g < ngroups) {
+    const int e0 = g * S::EPW;
+    const int nv = min(S::EPW, nelmt - e0);
+    for (int t = lane; t < nv * IDX; t += 32) {
+      const int ii = t / IDX, r = t - ii * IDX;
+      const int* src = (r < NEDOF) ? ge + (size_t)(e0 + ii) * NEDOF + r : pos + (size_t)(e0 + ii) * NGLL + (r - NEDOF);
+      cp_async4(buf + t, src);
+    }
+  }
+  cp_async_commit();
+}
 
 // Lane 0 issues chunk c of group g (all of its valid elements) into stage
 // c % NSTAGE; returns false when the group is past the end (nothing issued).
@@ -169,6 +198,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
   const int i = lane / KR, j = lane % KR;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + warp * NSTAGE;
   float* ring = reinterpret_cast<float*>(smem + S::BAR_BYTES) + (size_t)warp * S::RING_F;
+  int* ibuf = reinterpret_cast<int*>(smem + S::BAR_BYTES + (size_t)NW * S::RING_F * 4) + (size_t)warp * S::IBUF;
   const int ngroups = (nelmt + S::EPW - 1) / S::EPW;
   const int gstride = gridDim.x * NW;
   int g = blockIdx.x * NW + warp;
@@ -183,18 +213,26 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
   if (lane == 0)
     for (int c = 0; c < NSTAGE - 1; ++c) issued += issue_chunk<KR>(Ks, nelmt, ngroups, g, c, ring, bar);
   issued = __shfl_sync(0xffffffffu, issued, 0);
+  prefetch_indices<KR>(ge, pos, nelmt, ngroups, g, ibuf, lane);
   bool ok = true;
-  for (; g < ngroups && ok; g += gstride) {
+  for (int buf = 0; g < ngroups && ok; g += gstride, buf ^= 1) {
     const int e = g * S::EPW + i;
     const bool valid = e < nelmt;
+    // this group's indices have landed; the other buffer (read by the
+    // previous group) takes the next group's
+    cp_async_wait_all();
+    __syncwarp();
+    const int* idx = ibuf + buf * (S::EPW * IDX) + i * IDX;
+    prefetch_indices<KR>(ge, pos, nelmt, ngroups, g + gstride, ibuf + (buf ^ 1) * (S::EPW * IDX), lane);
     float p[NEDOF], y[NEDOF];
     {
-      const int* gp = ge + (size_t)(valid ? e : 0) * NEDOF;
+      const float* pj = pold + j;
+      const float* zj = z + j;
 #pragma unroll
       for (int r = 0; r < NEDOF; ++r) {
-        const int gd = valid ? __ldg(gp + r) : 0;
-        float pv = pold[(size_t)gd * KR + j];
-        if (combine) pv = fmaf(beta, pv, z[(size_t)gd * KR + j]);
+        const int gd = valid ? idx[r] : 0;
+        float pv = pj[(size_t)gd * KR];
+        if (combine) pv = fmaf(beta, pv, zj[(size_t)gd * KR]);
         p[r] = valid ? pv : 0.f;
         y[r] = 0.f;
       }
@@ -226,10 +264,9 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
     for_chunks(step, std::make_integer_sequence<int, NCH>{});
     if (!ok) break;
     if (valid) {
-      const int* pe = pos + (size_t)e * NGLL;
 #pragma unroll
       for (int a = 0; a < NGLL; ++a) {
-        const int q = __ldg(pe + a);
+        const int q = idx[NEDOF + a];
         if (q >= 0) {
           float* dst = Y + (size_t)q * 3 * KR + j;
           dst[0] = y[3 * a];
@@ -241,6 +278,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
   }
   // drain copies still in flight (after the last group they were never
   // issued; after a timeout this waits, bounded, for the warp's own copies)
+  cp_async_wait_all();
   issued = __shfl_sync(0xffffffffu, issued, 0);
   for (int q = waited; q < issued; ++q) mbar_wait(bar + (q % NCH) % NSTAGE, (unsigned)(((q % NCH) / NSTAGE) & 1));
 }

@@ -392,8 +392,10 @@ void launch_expand_dense(const double* Ks64, int nel, double* dense, const int* 
 // Element apply.
 // ---------------------------------------------------------------------------
 constexpr int APPLY_WARPS = 4;
-// 0 = register-staged loads, 1 = TMA bulk-copy pipeline (default)
-int g_apply_variant = 1;
+// 0 = register-staged loads, 1 = TMA bulk-copy pipeline (node lanes),
+// 2 = tensor cores (FP32, 8/16 RHS), 3 = lane per (element, RHS) for FP32
+// with 8/16 RHS and the TMA node-lane pipeline otherwise (default)
+int g_apply_variant = 3;
 void set_apply_variant(int v) { g_apply_variant = v; }
 // device copy of the stored-entry table, needed by the tensor-core apply
 const int* g_entry_dev = nullptr;
