@@ -289,6 +289,8 @@ sg_ctx* sg_create(int device, size_t hbm_budget) {
   // SG_APPLY_VARIANT selects another element apply for cross-checking:
   // 0 register-staged, 1 TMA node lanes, 2 tensor cores (default 3).
   if (const char* v = std::getenv("SG_APPLY_VARIANT")) set_apply_variant(std::atoi(v));
+  // SG_GATHER_VARIANT=0 selects the shared-memory-staged gather everywhere.
+  if (const char* v = std::getenv("SG_GATHER_VARIANT")) set_gather_variant(std::atoi(v));
   const KsTables& T = ks_tables();
   c->d_nbr = c->alloc<int>(NGLL * KS_NBR);
   c->d_entry = c->alloc<int>(KS_NNZ);

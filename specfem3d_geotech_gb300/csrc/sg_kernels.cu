@@ -884,9 +884,113 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
   }
 }
 
+// Row-cooperative gather for FP32 with KR = 4, 8 or 16: a node's slot rows
+// (3*KR floats) are read by LPN = 3*KR/4 lanes, one 16-byte piece each, so a
+// warp's loads are coalesced runs of Y and no shared memory is needed.  Lane
+// (node, q) sums piece q over the node's slots in element order -- the same
+// additions in the same order as the staged gather, so kp and p are bitwise
+// equal to it; the p.kp partials are compensated sums over the lane's four
+// columns, reduced in a fixed order.
+int g_gather_variant = 1;   // 0 = staged gather for every case
+void set_gather_variant(int v) { g_gather_variant = v; }
+
+template <int KR>
+__global__ void __launch_bounds__(RED_THREADS) k_pcg_gather_rows(
+    const int* __restrict__ ptr, const int* __restrict__ dof, int ng, const float* __restrict__ Y,
+    float* __restrict__ kp, float* __restrict__ p, const float* __restrict__ z, int mode, ColState* __restrict__ cs,
+    PcgGlobal* __restrict__ G, double* __restrict__ part) {
+  if (G->all_done) return;
+  constexpr int QPD = KR / 4;      // 16-byte pieces per dof row
+  constexpr int LPN = 3 * QPD;     // lanes per node
+  constexpr int NPW = 32 / LPN;    // nodes per warp
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nl = lane / LPN, q = lane - nl * LPN;
+  const int d = q / QPD, c0 = 4 * (q - d * QPD);
+  const bool act = nl < NPW;
+  DotAcc<float> dacc[4];
+  bool live[4];
+  float beta[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int j = act ? c0 + k : 0;
+    live[k] = act && cs[j].active && !cs[j].done;
+    beta[k] = (float)cs[j].beta;
+  }
+  const float4* yq = reinterpret_cast<const float4*>(Y) + q;
+  const int wstride = gridDim.x * GATHER_WARPS * NPW;
+  for (int g0 = (blockIdx.x * GATHER_WARPS + warp) * NPW; g0 < ng; g0 += wstride) {
+    const int g = g0 + nl;
+    if (!act || g >= ng) continue;
+    const int a = ptr[g], b = ptr[g + 1];
+    const int gd = dof[3 * g + d];
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int sl = a; sl < b; ++sl) {
+      const float4 v = __ldcs(yq + (size_t)sl * LPN);
+      acc.x = acc.x + v.x;
+      acc.y = acc.y + v.y;
+      acc.z = acc.z + v.z;
+      acc.w = acc.w + v.w;
+    }
+    if (!gd) continue;
+    float4* kpo = reinterpret_cast<float4*>(kp + (size_t)gd * KR + c0);
+    if (mode == 0) {
+      *kpo = acc;
+      continue;
+    }
+    float4* pp = reinterpret_cast<float4*>(p + (size_t)gd * KR + c0);
+    float4 pv = *pp;
+    const float4 zv = *reinterpret_cast<const float4*>(z + (size_t)gd * KR + c0);
+    if (live[0]) { pv.x = pdir(beta[0], pv.x, zv.x); dacc[0].add(pv.x, acc.x); }
+    if (live[1]) { pv.y = pdir(beta[1], pv.y, zv.y); dacc[1].add(pv.y, acc.y); }
+    if (live[2]) { pv.z = pdir(beta[2], pv.z, zv.z); dacc[2].add(pv.z, acc.z); }
+    if (live[3]) { pv.w = pdir(beta[3], pv.w, zv.w); dacc[3].add(pv.w, acc.w); }
+    *pp = pv;
+    *kpo = acc;
+  }
+  if (mode == 0) return;
+  __shared__ double sred[RED_THREADS / 32][KR];
+  double mine[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) mine[k] = act ? dacc[k].value() : 0.0;
+#pragma unroll
+  for (int j = 0; j < KR; ++j) {
+    double v = (act && (j >> 2) == (c0 >> 2)) ? mine[j & 3] : 0.0;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0) sred[warp][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < KR) {
+    double v = 0.0;
+    for (int w = 0; w < RED_THREADS / 32; ++w) v += sred[w][threadIdx.x];
+    part[(size_t)blockIdx.x * KR + threadIdx.x] = v;
+  }
+  if (last_block(&G->cntB)) {
+    __shared__ double sfin[RED_THREADS];
+    double v = 0.0;
+    for (int idx = threadIdx.x; idx < (int)gridDim.x * KR; idx += RED_THREADS) v += __ldcg(part + idx);
+    sfin[threadIdx.x] = v;
+    __syncthreads();
+    if (threadIdx.x < KR) {
+      int j = threadIdx.x;
+      double t = 0.0;
+      for (int u = j; u < RED_THREADS; u += KR) t += sfin[u];
+      if (cs[j].active && !cs[j].done) cs[j].alpha = cs[j].rz / t;
+    }
+    if (threadIdx.x == 0) G->cntB = 0;
+  }
+}
+
 template <typename V, int KR>
 void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mode, ColState* cs, PcgGlobal* G,
                 double* part, cudaStream_t s) {
+  if constexpr (std::is_same<V, float>::value && (KR == 4 || KR == 8 || KR == 16)) {
+    if (g_gather_variant == 1) {
+      SG_LAUNCH k_pcg_gather_rows<KR><<<NPART, RED_THREADS, 0, s>>>(T.d_ptr, T.d_dof, T.ngroups, Y, kp, p, z, mode,
+                                                                   cs, G, part);
+      return;
+    }
+  }
   constexpr size_t sm = GatherBuf<V, KR>::SMEM;
   static bool attr = false;
   if (!attr) {

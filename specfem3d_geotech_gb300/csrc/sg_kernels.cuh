@@ -54,6 +54,7 @@ template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
                         float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, cudaStream_t s);
 int apply_lanes_error_flag(cudaStream_t s);
+void set_gather_variant(int v);  // 1 row-cooperative gather for FP32 with 4/8/16 RHS (default), 0 staged
 template <typename V, int KR>
 // Y receives element slot (e, a)'s three rows (x KR) at the slot's gather
 // position pos[e*27+a] (slots of fully fixed nodes, pos < 0, are skipped).

@@ -291,7 +291,7 @@ def test_tensor_core_apply_matches_simt(ctx, tmp_path):
         assert rel(d["x"][t], x1[t]) <= MIXED_TOL
 
 
-def _variant_trials(variant, srfs, out):
+def _variant_trials(variant, srfs, out, var="SG_APPLY_VARIANT"):
     import subprocess
     import sys
     code = ("import sys; sys.path.insert(0, %r); import numpy as np; import specfem3d_geotech_gb300 as sg;"
@@ -299,7 +299,8 @@ def _variant_trials(variant, srfs, out):
             "r, x = m.trials(%r, sg.make_control(precision=sg.PREC_MIXED), want_x=True);"
             "np.savez(%r, x=x, nl=np.array([t['nl_iter'] for t in r]), cg=np.array([t['cg_tot'] for t in r]))") % (
         os.path.dirname(os.path.dirname(os.path.abspath(__file__))), srfs, str(out))
-    env = dict(os.environ, SG_APPLY_VARIANT=str(variant))
+    env = dict(os.environ)
+    env[var] = str(variant)
     subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=600)
     return np.load(out)
 
@@ -316,5 +317,19 @@ def test_lane_apply_matches_node_lane_apply(tmp_path, k):
     c = _variant_trials(3, srfs, tmp_path / "v3b.npz")
     assert a["nl"].tolist() == b["nl"].tolist()
     for t in range(k):
+        assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
+    assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
+
+
+def test_row_gather_matches_staged_gather(tmp_path):
+    """The row-cooperative FP32 gather (coalesced 16-byte pieces, no shared
+    memory) gives the staged gather's trials to the mixed-precision tolerance
+    with the same plastic-iteration counts; two runs of it are bitwise equal."""
+    srfs = [1.0 + 0.03 * t for t in range(8)]
+    a = _variant_trials(0, srfs, tmp_path / "g0.npz", var="SG_GATHER_VARIANT")
+    b = _variant_trials(1, srfs, tmp_path / "g1.npz", var="SG_GATHER_VARIANT")
+    c = _variant_trials(1, srfs, tmp_path / "g1b.npz", var="SG_GATHER_VARIANT")
+    assert a["nl"].tolist() == b["nl"].tolist()
+    for t in range(len(srfs)):
         assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
     assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
