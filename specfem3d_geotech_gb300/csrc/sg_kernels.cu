@@ -1047,6 +1047,66 @@ void launch_gather_plain(const GatherTopo& T, int KR, const V* Y, V* out, int ac
 // |alpha|*max|p|/max|u| <= tol (mode 0) or |r| <= tol*|r0| (mode 1), then
 // beta = r.z_new / r.z.
 // ---------------------------------------------------------------------------
+// Last block of an update: fixed-order reduction of the block partials and
+// the per-column stop test / beta (shared by both update kernels).
+template <int KR>
+__device__ __forceinline__ void update_finish(int init, ColState* __restrict__ cs, PcgGlobal* __restrict__ G,
+                                              const double* __restrict__ part) {
+  __shared__ int s_alldone;
+  __shared__ double sfin[RED_THREADS];
+  if (threadIdx.x == 0) s_alldone = 1;
+  // parallel fixed-order reduction of the block partials: thread t owns
+  // quantity t % (4*KR) of blocks t/(4*KR), t/(4*KR) + RED_THREADS/(4*KR), ...
+  {
+    constexpr int NQ = 4 * KR;
+    const int q = threadIdx.x % 4;
+    double v = 0.0;
+    for (int idx = threadIdx.x; idx < (int)gridDim.x * NQ; idx += RED_THREADS) {
+      double x = __ldcg(part + idx);
+      v = (q < 2) ? fmax(v, x) : v + x;
+    }
+    sfin[threadIdx.x] = v;
+  }
+  __syncthreads();
+  const int it = init ? 0 : G->it + 1;
+  if (threadIdx.x < KR) {
+    const int jj = threadIdx.x;
+    constexpr int NQ = 4 * KR;
+    ColState& c = cs[jj];
+    double a = 0.0, b = 0.0, s = 0.0, q = 0.0;
+    for (int t = jj * 4; t < RED_THREADS; t += NQ) {
+      a = fmax(a, sfin[t]); b = fmax(b, sfin[t + 1]); s += sfin[t + 2]; q += sfin[t + 3];
+    }
+    if (init) {
+      if (c.active) {
+        // keep_dir (G->mode & 2): continue the previous search direction after a
+        // residual replacement, beta = r.z_new / r.z of the last completed step
+        c.beta = (G->mode & 2) ? s / c.rz : 0.0;
+        c.rz = s; c.rr0 = q; c.rr = q; c.done = 0; c.failed = 0; c.iters = 0;
+      } else {
+        c.done = 1;
+      }
+    } else if (c.active && !c.done) {
+      c.maxp = a; c.maxu = b; c.rr = q;
+      bool stop = ((G->mode & 1) == 0) ? (fabs(c.alpha) * a / b <= c.tol) : (q <= c.tol * c.tol * c.rr0);
+      if (stop) {
+        c.done = 1; c.iters = it;
+      } else if (it >= G->maxiter) {
+        c.done = 1; c.failed = 1; c.iters = G->maxiter + 1;
+      } else {
+        c.beta = s / c.rz;
+        c.rz = s;
+      }
+    }
+    if (jj < G->kcols && c.active && !c.done) atomicAnd(&s_alldone, 0);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    G->it = it;
+    G->all_done = s_alldone;
+    G->cntC = 0;
+  }
+}
 template <typename V, int KR>
 __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
     int n1, V* __restrict__ u, V* __restrict__ r, V* __restrict__ z, const V* __restrict__ p,
@@ -1128,65 +1188,150 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_update(
     o[0] = a; o[1] = b; o[2] = c; o[3] = d;
   }
   if (!last_block(&G->cntC)) return;
-  __shared__ int s_alldone;
-  __shared__ double sfin[RED_THREADS];
-  if (threadIdx.x == 0) s_alldone = 1;
-  // parallel fixed-order reduction of the block partials: thread t owns
-  // quantity t % (4*KR) of blocks t/(4*KR), t/(4*KR) + RED_THREADS/(4*KR), ...
-  {
-    constexpr int NQ = 4 * KR;
-    const int q = threadIdx.x % 4;
-    double v = 0.0;
-    for (int idx = threadIdx.x; idx < (int)gridDim.x * NQ; idx += RED_THREADS) {
-      double x = __ldcg(part + idx);
-      v = (q < 2) ? fmax(v, x) : v + x;
-    }
-    sfin[threadIdx.x] = v;
+  update_finish<KR>(init, cs, G, part);
+}
+
+// FP32 update with KR = 4, 8 or 16 in 16-byte pieces: thread t always owns
+// columns c0..c0+3 (c0 = 4 (t mod KR/4)) of the rows it visits, so every load
+// moves 16 bytes; per-column max-norms and compensated dots are then reduced
+// over the lanes of equal c0 and finished exactly as in k_pcg_update.
+template <int KR>
+__global__ void __launch_bounds__(RED_THREADS, 4) k_pcg_update4(
+    int n1, float* __restrict__ u, float* __restrict__ r, float* __restrict__ z, const float* __restrict__ p,
+    const float* __restrict__ kp, const float* __restrict__ f, const float* __restrict__ dprecon, int init,
+    ColState* __restrict__ cs, PcgGlobal* __restrict__ G, double* __restrict__ part) {
+  if (G->all_done) return;
+  constexpr int QP = KR / 4;
+  const int c0 = 4 * (threadIdx.x % QP);
+  bool live[4];
+  float alpha[4];
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    live[k] = cs[c0 + k].active && (init || !cs[c0 + k].done);
+    alpha[k] = (float)(init ? 0.0 : cs[c0 + k].alpha);
+    any = any || live[k];
   }
-  __syncthreads();
-  const int it = init ? 0 : G->it + 1;
-  if (threadIdx.x < KR) {
-    const int jj = threadIdx.x;
-    constexpr int NQ = 4 * KR;
-    ColState& c = cs[jj];
-    double a = 0.0, b = 0.0, s = 0.0, q = 0.0;
-    for (int t = jj * 4; t < RED_THREADS; t += NQ) {
-      a = fmax(a, sfin[t]); b = fmax(b, sfin[t + 1]); s += sfin[t + 2]; q += sfin[t + 3];
-    }
+  const bool all4 = live[0] && live[1] && live[2] && live[3];
+  float mpv[4] = {0.f, 0.f, 0.f, 0.f}, muv[4] = {0.f, 0.f, 0.f, 0.f};
+  DotAcc<float> rza[4], rra[4];
+  if (any) {
+    const size_t n4 = (size_t)n1 * QP;                    // 16-byte pieces
+    const size_t stride = (size_t)gridDim.x * blockDim.x;  // a multiple of QP: c0 is fixed
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+    const float4* k4 = reinterpret_cast<const float4*>(kp);
+    float4* u4 = reinterpret_cast<float4*>(u);
+    float4* r4 = reinterpret_cast<float4*>(r);
+    float4* z4 = reinterpret_cast<float4*>(z);
     if (init) {
-      if (c.active) {
-        // keep_dir (G->mode & 2): continue the previous search direction after a
-        // residual replacement, beta = r.z_new / r.z of the last completed step
-        c.beta = (G->mode & 2) ? s / c.rz : 0.0;
-        c.rz = s; c.rr0 = q; c.rr = q; c.done = 0; c.failed = 0; c.iters = 0;
-      } else {
-        c.done = 1;
+      const float4* f4 = reinterpret_cast<const float4*>(f);
+      for (; i < n4; i += stride) {
+        const float4 fv = f4[i], kv = k4[i];
+        const float d = dprecon[i / QP];
+        float4 rn, zn;
+        rn.x = fv.x - kv.x; rn.y = fv.y - kv.y; rn.z = fv.z - kv.z; rn.w = fv.w - kv.w;
+        zn.x = d * rn.x; zn.y = d * rn.y; zn.z = d * rn.z; zn.w = d * rn.w;
+        const float rv[4] = {rn.x, rn.y, rn.z, rn.w}, zv[4] = {zn.x, zn.y, zn.z, zn.w};
+        if (all4) {
+          r4[i] = rn;
+          z4[i] = zn;
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (live[k]) { r[4 * i + k] = rv[k]; z[4 * i + k] = zv[k]; }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (live[k]) { rza[k].add(rv[k], zv[k]); rra[k].add(rv[k], rv[k]); }
       }
-    } else if (c.active && !c.done) {
-      c.maxp = a; c.maxu = b; c.rr = q;
-      bool stop = ((G->mode & 1) == 0) ? (fabs(c.alpha) * a / b <= c.tol) : (q <= c.tol * c.tol * c.rr0);
-      if (stop) {
-        c.done = 1; c.iters = it;
-      } else if (it >= G->maxiter) {
-        c.done = 1; c.failed = 1; c.iters = G->maxiter + 1;
-      } else {
-        c.beta = s / c.rz;
-        c.rz = s;
+    } else {
+      // four 16-byte loads per thread in flight, four CTAs per SM
+      constexpr int U = 1;
+      for (; i < n4; i += U * stride) {
+        float4 pv[U], uv[U], rv[U], kv[U];
+        float dv[U];
+        bool in[U];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+          const size_t o = i + q * stride;
+          in[q] = o < n4;
+          if (in[q]) { pv[q] = p4[o]; uv[q] = u4[o]; rv[q] = r4[o]; kv[q] = k4[o]; dv[q] = dprecon[o / QP]; }
+        }
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+          if (!in[q]) continue;
+          const size_t o = i + q * stride;
+          const float pa[4] = {pv[q].x, pv[q].y, pv[q].z, pv[q].w};
+          const float ua[4] = {uv[q].x, uv[q].y, uv[q].z, uv[q].w};
+          const float ra[4] = {rv[q].x, rv[q].y, rv[q].z, rv[q].w};
+          const float ka[4] = {kv[q].x, kv[q].y, kv[q].z, kv[q].w};
+          float un[4], rn[4], zn[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            un[k] = fmaf(alpha[k], pa[k], ua[k]);
+            rn[k] = fmaf(-alpha[k], ka[k], ra[k]);
+            zn[k] = dv[q] * rn[k];
+            if (live[k]) {
+              mpv[k] = fmaxf(mpv[k], fabsf(pa[k]));
+              muv[k] = fmaxf(muv[k], fabsf(un[k]));
+              rza[k].add(rn[k], zn[k]);
+              rra[k].add(rn[k], rn[k]);
+            }
+          }
+          if (all4) {
+            u4[o] = make_float4(un[0], un[1], un[2], un[3]);
+            r4[o] = make_float4(rn[0], rn[1], rn[2], rn[3]);
+            z4[o] = make_float4(zn[0], zn[1], zn[2], zn[3]);
+          } else {
+            // columns that are not live are left untouched
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              if (live[k]) { u[4 * o + k] = un[k]; r[4 * o + k] = rn[k]; z[4 * o + k] = zn[k]; }
+          }
+        }
       }
     }
-    if (jj < G->kcols && c.active && !c.done) atomicAnd(&s_alldone, 0);
+  }
+  __shared__ double sred[RED_THREADS / 32][KR][4];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double mp = (double)mpv[k], mu = (double)muv[k], rz = live[k] ? rza[k].value() : 0.0,
+           rr = live[k] ? rra[k].value() : 0.0;
+#pragma unroll
+    for (int o = 16; o >= QP; o >>= 1) {
+      mp = fmax(mp, __shfl_xor_sync(FULL, mp, o));
+      mu = fmax(mu, __shfl_xor_sync(FULL, mu, o));
+      rz += __shfl_xor_sync(FULL, rz, o);
+      rr += __shfl_xor_sync(FULL, rr, o);
+    }
+    if (lane < QP) {
+      const int j = 4 * lane + k;
+      sred[warp][j][0] = mp; sred[warp][j][1] = mu; sred[warp][j][2] = rz; sred[warp][j][3] = rr;
+    }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    G->it = it;
-    G->all_done = s_alldone;
-    G->cntC = 0;
+  if (threadIdx.x < KR) {
+    double a = 0.0, b = 0.0, c = 0.0, d = 0.0;
+    for (int w = 0; w < RED_THREADS / 32; ++w) {
+      a = fmax(a, sred[w][threadIdx.x][0]); b = fmax(b, sred[w][threadIdx.x][1]);
+      c += sred[w][threadIdx.x][2]; d += sred[w][threadIdx.x][3];
+    }
+    double* o = part + ((size_t)blockIdx.x * KR + threadIdx.x) * 4;
+    o[0] = a; o[1] = b; o[2] = c; o[3] = d;
   }
+  if (!last_block(&G->cntC)) return;
+  update_finish<KR>(init, cs, G, part);
 }
 
 template <typename V, int KR>
 void pcg_update(int n1, V* u, V* r, V* z, const V* p, const V* kp, const V* f, const V* dprecon, int init,
                 ColState* cs, PcgGlobal* G, double* part, cudaStream_t s) {
+  if constexpr (std::is_same<V, float>::value && (KR == 4 || KR == 8 || KR == 16)) {
+    SG_LAUNCH k_pcg_update4<KR><<<NPART, RED_THREADS, 0, s>>>(n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
+    return;
+  }
   SG_LAUNCH k_pcg_update<V, KR><<<NPART, RED_THREADS, 0, s>>>(n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
 }
 

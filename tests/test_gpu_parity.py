@@ -333,3 +333,19 @@ def test_row_gather_matches_staged_gather(tmp_path):
     for t in range(len(srfs)):
         assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
     assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
+
+
+def test_mixed_batch_of_eight_equals_single_trials(ctx, slope):
+    """Eight mixed-precision trials in one batch (lane apply, row gather and
+    16-byte update for 8 right-hand sides; columns finish at different PCG
+    iterations) give each trial's single-trial result (node-lane apply, staged
+    gather, scalar update) to the mixed-precision tolerance."""
+    mesh, _ = slope
+    m = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    ctl = sg.make_control(precision=sg.PREC_MIXED)
+    srfs = [1.0, 1.04, 1.08, 1.12, 1.16, 1.2, 1.24, 1.28]
+    res, xb = m.trials(srfs, ctl, want_x=True)
+    for t in (0, 3, 7):
+        (r1,), x1 = m.trials([srfs[t]], ctl, want_x=True)
+        assert res[t]["nl_iter"] == r1["nl_iter"]
+        assert rel(xb[t], x1[0]) <= MIXED_TOL
