@@ -229,9 +229,25 @@ def apply_kernel_name(kr: int) -> str:
     return f"k_apply_sparse_tma<float,{kr}>"
 
 
-def plain_fp64(sg, ctx, mesh, srf0, args):
+PREC_STEPS = 2               # plastic iterations compared by the precision leg
+
+
+def precision_report(r64, x64, r32, x32):
+    """Mixed batched vs plain FP64 after the same plastic iterations at the same SRF."""
+    import numpy as np
+    d = np.linalg.norm(x32 - x64) / np.linalg.norm(x64)
+    return {"plastic_iterations": PREC_STEPS, "srf": r64["srf"], "rel_l2_displacement": float(d),
+            "rel_umax": abs(r32["umax"] - r64["umax"]) / abs(r64["umax"]),
+            "rel_fmax": abs(r32["fmax"] - r64["fmax"]) / max(abs(r64["fmax"]), 1e-300),
+            "pcg_iters_fp64": r64["cg_tot"], "inner_pcg_iters_mixed": r32["cg_tot"],
+            "pcg_inflation": r32["cg_tot"] / max(1, r64["cg_tot"]), "refine_rounds_mixed": r32["refine_steps"],
+            "tolerance": 1e-6, "within_tolerance": bool(d <= 1e-6)}
+
+
+def plain_fp64(sg, ctx, mesh, srf0, args, want_x=False):
     """Plain FP64 one-at-a-time trial on the same mesh: trial plastic iterations/s
-    and PCG iterations per plastic iteration of the reference algorithm."""
+    and PCG iterations per plastic iteration of the reference algorithm (and,
+    for the precision leg, the trial's first PREC_STEPS plastic iterations)."""
     m64 = sg.Model(mesh, precision=sg.PREC_FP64, ctx=ctx)
     c64 = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=NL_MAXITER)
     m64.batch_begin(c64, 1)
@@ -245,9 +261,14 @@ def plain_fp64(sg, ctx, mesh, srf0, args):
     t64 = ctx.elapsed_ms(4, 5)
     a64 = m64.batch_poll(0)[1]
     m64.batch_end()
+    px = None
+    if want_x:
+        cp = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=PREC_STEPS)
+        (r, ), x = m64.trials([srf0], cp, want_x=True)
+        px = (r, x[0])
     m64.close()
     steps64 = a64["nl_iter"] - b64["nl_iter"]
-    return steps64 / (t64 / 1000.0), (a64["cg_tot"] - b64["cg_tot"]) / max(1, steps64)
+    return steps64 / (t64 / 1000.0), (a64["cg_tot"] - b64["cg_tot"]) / max(1, steps64), px
 
 
 def end_to_end(sg, ctx, mesh, ctl, srf, k, args, world):
@@ -308,6 +329,13 @@ def run_ours(args, rank, world, local):
     slot_steps = sum(a["nl_iter"] - b["nl_iter"] for a, b in zip(after, before))
     cg = sum(a["cg_tot"] - b["cg_tot"] for a, b in zip(after, before))
     model.batch_end()
+    prec32 = None
+    if not args.no_fp64:
+        # config-2 precision report: the same batch of k trials, first PREC_STEPS plastic iterations
+        cp = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=PREC_STEPS,
+                             precision=sg.PREC_MIXED)
+        r, x = model.trials(srf, cp, want_x=True)
+        prec32 = (r[0], x[0])
     t_max = barrier_max(t_ms, world)
     rate_all = slot_steps / (t_max / 1000.0) * world         # trial plastic iterations / s, all ranks
     value = rate_all / FOS_WORK
@@ -328,11 +356,13 @@ def run_ours(args, rank, world, local):
         with open(tpath) as f:
             traffic = json.load(f).get("bytes_per_launch")
 
+    precision = None
     if args.no_fp64:
         rate64, n_cg_ref = float("nan"), N_CG_REF
     else:
-        rate64, n_cg_ref = plain_fp64(sg, ctx, mesh, srf[0], args)
+        rate64, n_cg_ref, prec64 = plain_fp64(sg, ctx, mesh, srf[0], args, want_x=True)
         rate64 *= world
+        precision = precision_report(prec64[0], prec64[1], prec32[0], prec32[1])
     if args.no_e2e:
         e2e = None
     else:
@@ -356,6 +386,7 @@ def run_ours(args, rank, world, local):
         "fp64_plain": {"trial_plastic_iters_per_s": rate64, "value": rate64 / FOS_WORK,
                        "pcg_iters_per_plastic_iter": n_cg_ref,
                        "mixed_batched_over_plain": rate_all / rate64 if rate64 == rate64 else None},
+        "precision": precision,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": apply_kernel_name(kr),
                      "algorithmic_bytes_per_launch": bytes_apply, "avg_launch_ms": apply_ms,

@@ -156,9 +156,15 @@ def test_mixed_precision_within_tolerance(ctx, slope):
     c64 = sg.make_control()
     c32 = sg.make_control(precision=sg.PREC_MIXED)
     (r64,), x64 = m64.trials([1.0], c64, want_x=True)
+    s64 = m64.last_stress(0)
     (r32,), x32 = m32.trials([1.0], c32, want_x=True)
+    s32 = m32.last_stress(0)
     assert r32["nl_iter"] == r64["nl_iter"]
     assert rel(x32[0], x64[0]) <= MIXED_TOL
+    # converged stress state (stored at convergence, src/slope.F90:377-381)
+    serr = np.abs(s32 - s64).max() / np.abs(s64).max()
+    print(f"mixed vs FP64: displacement {rel(x32[0], x64[0]):.2e}, stress {serr:.2e}")
+    assert serr <= 1e-5
     assert r32["refine_steps"] >= r32["nl_iter"]
 
 
