@@ -612,8 +612,11 @@ double maxabs(const double* v, int n1) {
   return m;
 }
 // Dot-product summation order: 0 = sequential (the reference's dot_product),
-// 1 = pairwise halving.  The second order exists only to measure how far
-// rounding alone moves a PCG solve (the parity noise floor); it is never the default.
+// 1 = pairwise halving, 2 = 13 interleaved partial sums (a strided split like
+// a GPU grid-stride loop), 3 = reverse sequential, 100 + m = m interleaved
+// partial sums.  Orders other than 0 exist only to measure how far rounding
+// alone moves a solve or a trial (the parity noise floor); they are never the
+// default.
 int g_dot_order = 0;
 double dot_pairwise(const double* a, const double* b, int n) {
   if (n <= 8) {
@@ -626,6 +629,20 @@ double dot_pairwise(const double* a, const double* b, int n) {
 }
 double dot(const double* a, const double* b, int n1) {
   if (g_dot_order == 1) return dot_pairwise(a, b, n1);
+  if (g_dot_order == 2 || g_dot_order >= 100) {
+    // m interleaved partial sums (order 2: m = 13; order 100 + m: m in 1..256)
+    const int m = g_dot_order == 2 ? 13 : std::min(256, std::max(1, g_dot_order - 100));
+    double part[256] = {0.0};
+    for (int i = 0; i < n1; ++i) part[i % m] = part[i % m] + a[i] * b[i];
+    double s = 0.0;
+    for (int k = 0; k < m; ++k) s = s + part[k];
+    return s;
+  }
+  if (g_dot_order == 3) {
+    double s = 0.0;
+    for (int i = n1 - 1; i >= 0; --i) s = s + a[i] * b[i];
+    return s;
+  }
   double s = 0.0;
   for (int i = 0; i < n1; ++i) s = s + a[i] * b[i];
   return s;

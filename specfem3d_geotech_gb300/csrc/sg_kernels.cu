@@ -771,6 +771,15 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
 // directly from global memory.
 constexpr int GATHER_WARPS = RED_THREADS / 32;
 
+// Grid of a PCG kernel with a last-block reduction: enough blocks for `per`
+// items each, at most `cap`.  Small problems get few blocks, so the last
+// block sums few partials; the grid depends only on the problem size, so the
+// reduction order (and the result) stays fixed for a given problem.
+static inline int red_grid(size_t items, size_t per, int cap) {
+  size_t g = (items + per - 1) / per;
+  return (int)std::max<size_t>(1, std::min<size_t>(g, (size_t)cap));
+}
+
 template <typename V, int KR>
 struct GatherBuf {
   static constexpr int ROW = 3 * KR;                                    // values per slot
@@ -990,7 +999,8 @@ void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mo
     if (g_gather_variant == 1) {
       // five resident CTAs per SM (register-limited), one wave: measured
       // 0.244 ms against 0.279 ms with four per SM on the 192k-element slope
-      SG_LAUNCH k_pcg_gather_rows<KR><<<GATHER_ROWS_BLOCKS, RED_THREADS, 0, s>>>(T.d_ptr, T.d_dof, T.ngroups, Y, kp, p, z, mode,
+      constexpr int NPB = GATHER_WARPS * (32 / (3 * KR / 4));   // nodes per block and pass
+      SG_LAUNCH k_pcg_gather_rows<KR><<<red_grid(T.ngroups, NPB * 4, GATHER_ROWS_BLOCKS), RED_THREADS, 0, s>>>(T.d_ptr, T.d_dof, T.ngroups, Y, kp, p, z, mode,
                                                                    cs, G, part);
       return;
     }
@@ -1001,7 +1011,7 @@ void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mo
     cudaFuncSetAttribute(k_pcg_gather<V, KR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     attr = true;
   }
-  SG_LAUNCH k_pcg_gather<V, KR><<<NPART, RED_THREADS, sm, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, Y, kp, p, z, mode,
+  SG_LAUNCH k_pcg_gather<V, KR><<<red_grid(T.ngroups, GATHER_WARPS * 32 * 2, NPART), RED_THREADS, sm, s>>>(T.d_ptr, T.d_ent, T.d_dof, T.ngroups, Y, kp, p, z, mode,
                                                               cs, G, part);
 }
 
@@ -1329,10 +1339,12 @@ template <typename V, int KR>
 void pcg_update(int n1, V* u, V* r, V* z, const V* p, const V* kp, const V* f, const V* dprecon, int init,
                 ColState* cs, PcgGlobal* G, double* part, cudaStream_t s) {
   if constexpr (std::is_same<V, float>::value && (KR == 4 || KR == 8 || KR == 16)) {
-    SG_LAUNCH k_pcg_update4<KR><<<NPART, RED_THREADS, 0, s>>>(n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
+    SG_LAUNCH k_pcg_update4<KR><<<red_grid((size_t)n1 * (KR / 4), RED_THREADS * 4, NPART), RED_THREADS, 0, s>>>(
+        n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
     return;
   }
-  SG_LAUNCH k_pcg_update<V, KR><<<NPART, RED_THREADS, 0, s>>>(n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
+  SG_LAUNCH k_pcg_update<V, KR><<<red_grid((size_t)n1 * KR, RED_THREADS * 4, NPART), RED_THREADS, 0, s>>>(
+      n1, u, r, z, p, kp, f, dprecon, init, cs, G, part);
 }
 
 // ---------------------------------------------------------------------------

@@ -2,12 +2,13 @@
 
 Tolerances: a single FP64 PCG solve must match the oracle's displacement to
 relative L2 <= 1e-8 (the PCG step tolerance); a whole plastic trial to 5e-8
-with identical plastic-iteration counts, 2e-6 on stresses and 2e-3 on fmax.
-These are twice the oracle's own rounding noise floor: the oracle moves by
-5e-9 (one solve) and 2.3e-8 / 5e-7 / 5e-4 (a trial's x / stress / fmax) when
-only the summation order of its dot products changes
-(tests/test_oracle_kat.py::test_pcg_rounding_noise_floor and
-test_trial_rounding_noise_floor), so tighter bounds would test rounding
+with identical plastic-iteration counts, 2e-5 on stresses and 2e-3 on fmax.
+These are about twice the oracle's own rounding noise floor: the oracle moves
+by 5e-9 (one solve) and 4e-8 / 8.7e-6 / 8e-4 (a trial's x / stress / fmax)
+when only the summation order of its dot products changes -- the stress
+figure is a yield decision at a GLL point near F = 0 that flips with the
+order (tests/test_oracle_kat.py::test_pcg_rounding_noise_floor and
+test_trial_rounding_noise_floor) -- so tighter bounds would test rounding
 order, not the algorithm.  The mixed FP32/FP64 refinement form must stay within
 1e-6 of the FP64 result.  Integer outputs (node numbering, dof maps) must be
 identical.
@@ -26,7 +27,7 @@ pytestmark = pytest.mark.gpu
 
 FP64_TOL = 1e-8
 TRIAL_TOL = 5e-8
-STRESS_TOL = 2e-6
+STRESS_TOL = 2e-5
 FMAX_TOL = 2e-3
 MIXED_TOL = 1e-6
 

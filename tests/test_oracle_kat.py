@@ -205,19 +205,27 @@ def test_pcg_rounding_noise_floor():
 
 
 def test_trial_rounding_noise_floor():
-    """A whole plastic trial (SRF 1.0, 12 plastic iterations) moves by ~2e-8 in x
-    and ~5e-7 in stress when only the dot-product summation order changes."""
+    """How far rounding alone moves a plastic trial: only the dot-product
+    summation order of the oracle changes (sequential, pairwise, strided
+    partial sums, reverse).  At SRF 1.0 (12 plastic iterations) x moves by
+    ~2e-8 and stress by < 1e-6; at SRF 1.1 (22 plastic iterations) some orders
+    flip the yield decision of a GLL point near F = 0 and move the converged
+    stress by 8.7e-6 (fmax by up to 8e-4) while x stays within 4e-8."""
     om = OracleModel(meshgen.slope2d())
-    out = []
     try:
-        for order in (0, 1):
-            L.orc_set_dot_order(order)
-            out.append(om.trial(1.0, want_x=True, want_stress=True))
+        for srf, orders, ds_max in ((1.0, (1, 2, 3), 1e-6), (1.1, (1, 3, 128, 164), 1e-5)):
+            L.orc_set_dot_order(0)
+            a = om.trial(srf, want_x=True, want_stress=True)
+            spread = []
+            for order in orders:
+                L.orc_set_dot_order(order)
+                b = om.trial(srf, want_x=True, want_stress=True)
+                assert a["nl_iter"] == b["nl_iter"]
+                dx = np.linalg.norm(a["x"] - b["x"]) / np.linalg.norm(a["x"])
+                assert 1e-10 < dx < 5e-8
+                spread.append(np.abs(a["stress"] - b["stress"]).max() / np.abs(a["stress"]).max())
+            assert max(spread) < ds_max
+            if srf == 1.1:
+                assert max(spread) > 5e-6     # the yield-flip mode is reached by some orders
     finally:
         L.orc_set_dot_order(0)
-    a, b = out
-    assert a["nl_iter"] == b["nl_iter"]
-    dx = np.linalg.norm(a["x"] - b["x"]) / np.linalg.norm(a["x"])
-    ds = np.abs(a["stress"] - b["stress"]).max() / np.abs(a["stress"]).max()
-    assert 1e-10 < dx < 5e-8
-    assert ds < 2e-6
