@@ -244,6 +244,53 @@ def precision_report(r64, x64, r32, x32):
             "tolerance": 1e-6, "within_tolerance": bool(d <= 1e-6)}
 
 
+def serving_leg(sg, args):
+    """Config 4 scaled to a bounded run: a seeded Poisson stream of FOS requests
+    (random slopes, log-uniform mesh sizes, k = 4..16 concurrent trials) through
+    the request loop, once in the mixed batched form (4 workers, continuous
+    batching) and once as plain FP64 one at a time (1 worker, bisection, k = 1).
+    Both arms see the same requests and the same nl_maxiter."""
+    import numpy as np
+    from specfem3d_geotech_gb300 import meshgen
+    rng = np.random.default_rng(4)
+    n = args.serve
+    sizes = np.exp(rng.uniform(math.log(args.serve_min), math.log(args.serve_max), n)).astype(int)
+    meshes = [meshgen.random_slope(rng, int(sz)) for sz in sizes]
+    ks = rng.integers(4, 17, n)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, n))
+
+    def run(prec, kof, workers):
+        ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=args.serve_nl, precision=prec)
+        srv = sg.Server(0, 0, workers=workers)
+        t0 = time.perf_counter()
+        ids = []
+        for i, m in enumerate(meshes):
+            dt = arrivals[i] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(srv.submit(m, ctl, lo=1.0, hi=3.0, step=0.01, k=kof(i)))
+        res = [srv.wait(r, timeout=7200) for r in ids]
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        lat = [r["t_done"] - r["t_arrival"] for r in res]
+        return res, {"solves_per_s": len(res) / wall, "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+                     "mean_s": float(np.mean(lat)), "peak_concurrent": st["peak_concurrent"],
+                     "trials": int(sum(r["ntrials"] for r in res)), "wall_s": wall,
+                     "ok": all(r["status"] == 0 for r in res)}
+
+    rm, mixed = run(sg.PREC_MIXED, lambda i: int(ks[i]), 4)
+    rp, plain = run(sg.PREC_FP64, lambda i: 1, 1)
+    same = sum(1 for a, b in zip(rm, rp) if a["fos"] == b["fos"])
+    return {"requests": n, "rate_per_s": args.serve_rate, "nelmt": [int(r["nelmt"]) for r in rm],
+            "k": [int(k) for k in ks], "nl_maxiter": args.serve_nl,
+            "srf_grid": "k-section (mixed) / bisection (plain) on [1, 3] to 0.01",
+            "mixed_batched": mixed, "plain_fp64_one_at_a_time": plain,
+            "solves_per_s_ratio": mixed["solves_per_s"] / plain["solves_per_s"],
+            "same_critical_srf": f"{same}/{n}", "fos_mixed": [r["fos"] for r in rm],
+            "fos_plain": [r["fos"] for r in rp]}
+
+
 def plain_fp64(sg, ctx, mesh, srf0, args, want_x=False):
     """Plain FP64 one-at-a-time trial on the same mesh: trial plastic iterations/s
     and PCG iterations per plastic iteration of the reference algorithm (and,
@@ -399,6 +446,8 @@ def run_ours(args, rank, world, local):
         "clocks": clk,
         "e2e": e2e,
     }
+    if rank == 0 and args.serve > 0:
+        line["serving"] = serving_leg(sg, args)
     if rank == 0 and not args.no_cpu:
         t0 = time.time()
         r = oracle_sample(n_cg=n_cg_ref, iters=CPU_SAMPLE_ITERS)
@@ -426,6 +475,11 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--nx", type=int, default=120, help="elements along x (120 = the 192k-element mesh)")
+    ap.add_argument("--serve", type=int, default=6, help="requests in the serving leg (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving leg (1/s)")
+    ap.add_argument("--serve-min", type=int, default=300, help="smallest request mesh (elements)")
+    ap.add_argument("--serve-max", type=int, default=3000, help="largest request mesh (elements)")
+    ap.add_argument("--serve-nl", type=int, default=100, help="nl_maxiter of the serving requests")
     args = ap.parse_args()
     rank, world, local = dist()
     if args.impl == "reference":
