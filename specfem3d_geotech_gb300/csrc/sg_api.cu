@@ -507,6 +507,7 @@ struct sg_model {
   GatherTopo T;
   double* d_K64 = nullptr;
   float* d_K32 = nullptr;
+  float* d_rec32 = nullptr;  // matrix-free FP32 operator: per GLL point J^-1 and w detJ C (MF_REC floats)
   double *d_diag = nullptr, *d_dprecon = nullptr, *d_extload = nullptr;
   float* d_dprecon32 = nullptr;
   double* d_Yscratch = nullptr;  // nelmt*81 (diag / gravity element vectors)
@@ -575,6 +576,7 @@ static bool model_stiffness(sg_model* M, const int* d_elist, int nel, const doub
   int ev = c->prof_begin();
   launch_stiffness(M->d_geo, M->d_matid, d_elist, nel, M->d_ym, d_nuv, M->d_gam, M->d_K64, M->d_K32, Ydiag,
                    gravity ? Ygrav : nullptr, c->d_entry, T.d_pos, s);
+  launch_mf_record(M->d_geo, M->d_matid, d_elist, nel, M->d_ym, d_nuv, M->d_rec32, s);
   c->prof_end(ev, 5);
   cudaMemsetAsync(M->d_diag, 0, sizeof(double) * n1, s);
   launch_gather_plain<double>(T, 1, Ydiag, M->d_diag, 0, nullptr, s);
@@ -621,6 +623,7 @@ static sg_model* model_build(sg_ctx* c, HostMesh&& H, int nnode8, const double* 
   M->d_K64 = c->alloc<double>((size_t)ne * KS_STRIDE);
   if (precision == SG_PREC_MIXED) {
     M->d_K32 = c->alloc<float>((size_t)ne * KS_STRIDE);
+    M->d_rec32 = c->alloc<float>((size_t)ne * NGLL * MF_REC);
     M->d_dprecon32 = c->alloc<float>(n1);
   }
   M->d_diag = c->alloc<double>(n1);
@@ -630,7 +633,7 @@ static sg_model* model_build(sg_ctx* c, HostMesh&& H, int nnode8, const double* 
   M->d_fpart = c->alloc<double>(NPART * 2);
   bool ok = M->d_coord && M->d_gnum && M->d_matid && M->d_ge && M->d_gdof && M->d_ym && M->d_nu && M->d_gam &&
             M->d_geo && M->d_K64 && M->d_diag && M->d_dprecon && M->d_extload && M->d_Yscratch && M->d_fpart &&
-            (precision == SG_PREC_FP64 || (M->d_K32 && M->d_dprecon32)) && upload_topo(c, M->T);
+            (precision == SG_PREC_FP64 || (M->d_K32 && M->d_rec32 && M->d_dprecon32)) && upload_topo(c, M->T);
   if (!ok) {
     set_tag(errtag, "ERROR: the model does not fit the device memory budget!");
     sg_model_free(M);
@@ -709,7 +712,7 @@ void sg_model_free(sg_model* M) {
   free_topo(c, M->T);
   for (void* p : {(void*)M->d_coord, (void*)M->d_gnum, (void*)M->d_matid, (void*)M->d_ge, (void*)M->d_gdof,
                   (void*)M->d_ym, (void*)M->d_nu, (void*)M->d_gam, (void*)M->d_geo, (void*)M->d_K64, (void*)M->d_K32,
-                  (void*)M->d_diag, (void*)M->d_dprecon, (void*)M->d_extload, (void*)M->d_dprecon32,
+                  (void*)M->d_rec32, (void*)M->d_diag, (void*)M->d_dprecon, (void*)M->d_extload, (void*)M->d_dprecon32,
                   (void*)M->d_Yscratch, (void*)M->d_fpart})
     c->release(p);
   delete M;
@@ -840,6 +843,18 @@ struct SolveStats {
   int iters[16];
   int refine = 0;
 };
+
+// The FP32 operator of the mixed solve: the stored FP32 element matrices, or
+// the matrix-free form from the per-point records.
+static Op fp32_op(const sg_model* M, const Op& op64) {
+  Op o = op64;
+  o.K = M->d_K32;
+  if (fp32_matrix_free()) {
+    o.dense = 2;
+    o.K = M->d_rec32;
+  }
+  return o;
+}
 
 static int linear_solve(sg_model* M, const sg_control* ctl, const Op& op64, const Op& op32, int k,
                         const std::vector<int>& active, SolveStats& S, const double* dprecon, const float* dprecon32) {
@@ -1018,8 +1033,7 @@ static int batch_iteration(sg_model* M) {
   if (!any) return SG_OK;
   Op op64, op32;
   op64.K = M->d_K64; op64.ge = M->d_ge; op64.nelmt = ne; op64.T = &M->T;
-  op32 = op64;
-  op32.K = M->d_K32;
+  op32 = fp32_op(M, op64);
   launch_load_combine(n1, KR, M->d_extload, W.bodyload, W.load, s);
   SolveStats St;
   int st = linear_solve(M, ctl, op64, op32, k, live, St, M->d_dprecon, M->d_dprecon32);
@@ -1262,7 +1276,7 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
       cudaMemcpyAsync(M->W.load, M->d_extload, sizeof(double) * n1, cudaMemcpyDeviceToDevice, s);
       Op op64, op32;
       op64.K = M->d_K64; op64.ge = M->d_ge; op64.nelmt = ne; op64.T = &M->T;
-      op32 = op64; op32.K = M->d_K32;
+      op32 = fp32_op(M, op64);
       SolveStats S;
       std::vector<int> act(1, 1);
       status = linear_solve(M, &c0, op64, op32, 1, act, S, M->d_dprecon, M->d_dprecon32);
@@ -1353,7 +1367,7 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
         c->release(d_nuf);
         Op op64, op32;
         op64.K = M->d_K64; op64.ge = d_geint; op64.nelmt = nint; op64.T = &Ti;
-        op32 = op64; op32.K = M->d_K32;
+        op32 = fp32_op(M, op64);
         int cg_tot = 0, nl_tot = 0, nl_iter = 0;
         double fmax = 0.0, red[64];
         for (int inc = 0; inc < ninc && status == SG_OK; ++inc) {

@@ -1,0 +1,221 @@
+// sg_apply_mf.cu -- matrix-free FP32 element apply of the mixed form.
+//
+// With GLL quadrature at the 27 element nodes the stored element matrix is
+//   K_e = sum_q w_q detJ_q B_q^T C B_q        (src/preprocess.f90:74-148),
+// so K_e p can be formed without K_e: at every GLL point q take the gradient
+// of p (each reference derivative is a 3-term sum along one lattice line,
+// with the 1D GLL derivative matrix D), map it with J^-1, form the stress
+// sigma = C eps with the engineering shears of compute_bmat
+// (src/preprocess.f90:12-68) and the isotropic C of compute_cmat
+// (src/elastic.f90:13-42), and return it through B_q^T (again 3-term line
+// sums).  Per element this reads a 48-byte record per GLL point (J^-1 and the
+// three C constants scaled by w_q detJ_q, 1.3 KB per element) instead of the
+// 9.7 KB of stored FP32 entries, and costs about 3,600 FMAs per right-hand
+// side against 4,617.
+//
+// Thread (element, node a, trial j): gathers p at node a (combined with z on
+// the fly), forms the stress fluxes at GLL point a, then the result rows of
+// node a; the element's p and fluxes live in shared memory between the two
+// phases.  The FP64 residual of the mixed solve keeps the stored FP64
+// matrices, so this operator only steers the FP32 inner iterations.
+#include <cstdint>
+
+#include "sg_kernels.cuh"
+
+namespace sg {
+
+namespace mf {
+
+constexpr int REC = MF_REC;  // floats per GLL point: J^-1 row-major, w detJ c11, w detJ c12, w detJ c44
+
+// D[i][t] = derivative of the 1D Lagrange basis t at GLL point i (nodes -1, 0, 1)
+__device__ __forceinline__ constexpr float Dm(int i, int t) {
+  return i == 0 ? (t == 0 ? -1.5f : t == 1 ? 2.0f : -0.5f)
+                : i == 1 ? (t == 0 ? -0.5f : t == 1 ? 0.0f : 0.5f) : (t == 0 ? 0.5f : t == 1 ? -2.0f : 1.5f);
+}
+
+template <int KR>
+struct Shape {
+  static constexpr int TPE = NGLL * KR;                       // threads per element
+  static constexpr int EPC = TPE >= 216 ? 1 : 216 / TPE;      // elements per CTA
+  static constexpr int NT = ((EPC * TPE + 31) / 32) * 32;     // CTA threads
+  static constexpr int UF = NEDOF * KR;                       // p values per element
+  static constexpr int SF = NGLL * 9 * KR;                    // flux values per element
+};
+
+// Gradient of the three components along the lattice lines through point a:
+// g[c][r] = sum_t D[i_r][t] u_c(node with index t in direction r).
+template <int KR>
+__device__ __forceinline__ void ref_grad(const float* __restrict__ U, int a, int j, float g[3][3]) {
+  const int ic[3] = {a % 3, (a / 3) % 3, a / 9};
+  const int st[3] = {1, 3, 9};
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int base = a - ic[r] * st[r];
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+      const float d = Dm(ic[r], t);
+      const float* u = U + (size_t)(3 * (base + t * st[r])) * KR + j;
+      s0 = fmaf(d, u[0], s0);
+      s1 = fmaf(d, u[KR], s1);
+      s2 = fmaf(d, u[2 * KR], s2);
+    }
+    g[0][r] = s0;
+    g[1][r] = s1;
+    g[2][r] = s2;
+  }
+}
+
+template <int KR>
+__global__ void __launch_bounds__(Shape<KR>::NT) k_apply_mf(
+    const float* __restrict__ rec, const int* __restrict__ ge, int nelmt, const float* __restrict__ pold,
+    const float* __restrict__ z, int combine, float* __restrict__ Y, const ColState* __restrict__ cs,
+    const PcgGlobal* __restrict__ G, const int* __restrict__ pos) {
+  using S = Shape<KR>;
+  if (G && G->all_done) return;
+  __shared__ __align__(16) float sU[S::EPC][S::UF];
+  __shared__ __align__(16) float sS[S::EPC][S::SF];
+  const int t = threadIdx.x;
+  const int el = t / S::TPE, rem = t - el * S::TPE;
+  const int a = rem / KR, j = rem - a * KR;
+  const bool act = el < S::EPC;
+  const float beta = (act && combine) ? (float)cs[j].beta : 0.f;
+  float* U = sU[act ? el : 0];
+  float* F = sS[act ? el : 0];
+  for (int e0 = blockIdx.x * S::EPC; e0 < nelmt; e0 += gridDim.x * S::EPC) {
+    const int e = e0 + el;
+    const bool valid = act && e < nelmt;
+    if (act) {
+      float u[3] = {0.f, 0.f, 0.f};
+      if (valid) {
+        const int* g = ge + (size_t)e * NEDOF + 3 * a;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int gd = __ldg(g + c);
+          float pv = pold[(size_t)gd * KR + j];
+          if (combine) pv = fmaf(beta, pv, z[(size_t)gd * KR + j]);
+          u[c] = pv;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) U[(3 * a + c) * KR + j] = u[c];
+    }
+    __syncthreads();
+    if (valid) {
+      float gr[3][3];
+      ref_grad<KR>(U, a, j, gr);
+      const float4* R = reinterpret_cast<const float4*>(rec + ((size_t)e * NGLL + a) * REC);
+      const float4 r0 = __ldg(R), r1 = __ldg(R + 1), r2 = __ldg(R + 2);
+      const float Ji[9] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x};
+      const float c11 = r2.y, c12 = r2.z, c44 = r2.w;
+      // physical gradient gp[c][d] = du_c/dx_d = sum_r Ji[3d+r] gr[c][r]
+      float gp[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          gp[c][d] = fmaf(Ji[3 * d], gr[c][0], fmaf(Ji[3 * d + 1], gr[c][1], Ji[3 * d + 2] * gr[c][2]));
+      // stress (already weighted by w detJ): normal from c11, c12; shears c44 x engineering strain
+      const float exx = gp[0][0], eyy = gp[1][1], ezz = gp[2][2];
+      float T[3][3];
+      T[0][0] = fmaf(c11, exx, c12 * (eyy + ezz));
+      T[1][1] = fmaf(c11, eyy, c12 * (exx + ezz));
+      T[2][2] = fmaf(c11, ezz, c12 * (exx + eyy));
+      T[0][1] = T[1][0] = c44 * (gp[0][1] + gp[1][0]);
+      T[1][2] = T[2][1] = c44 * (gp[1][2] + gp[2][1]);
+      T[0][2] = T[2][0] = c44 * (gp[0][2] + gp[2][0]);
+      // fluxes F[c][r] = sum_d Ji[3d+r] T[c][d]
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          F[((3 * a + c) * 3 + r) * KR + j] =
+              fmaf(Ji[r], T[c][0], fmaf(Ji[3 + r], T[c][1], Ji[6 + r] * T[c][2]));
+    }
+    __syncthreads();
+    if (valid) {
+      // rows of node a: y_c(a) = sum_r sum_t D[t][i_r(a)] F_(point t on line r)[c][r]
+      const int ic[3] = {a % 3, (a / 3) % 3, a / 9};
+      const int st[3] = {1, 3, 9};
+      float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const int base = a - ic[r] * st[r];
+#pragma unroll
+        for (int tt = 0; tt < 3; ++tt) {
+          const float d = Dm(tt, ic[r]);
+          const float* f = F + (size_t)((3 * (base + tt * st[r])) * 3 + r) * KR + j;
+          y0 = fmaf(d, f[0], y0);
+          y1 = fmaf(d, f[3 * KR], y1);
+          y2 = fmaf(d, f[6 * KR], y2);
+        }
+      }
+      const int q = pos[(size_t)e * NGLL + a];
+      if (q >= 0) {
+        float* dst = Y + (size_t)q * 3 * KR + j;
+        dst[0] = y0;
+        dst[KR] = y1;
+        dst[2 * KR] = y2;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Record of GLL point q of operator element le (element elist[le]):
+// J^-1 (row-major, as cached by the geometry kernel) and the compute_cmat
+// constants times w_q detJ_q, rounded to FP32.
+__global__ void k_mf_record(const double* __restrict__ geo, const int* __restrict__ mat_id,
+                            const int* __restrict__ elist, int nel, const double* __restrict__ ym,
+                            const double* __restrict__ nu, float* __restrict__ rec) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= nel * NGLL) return;
+  const int le = tid / NGLL, q = tid - le * NGLL;
+  const int e = elist ? elist[le] : le;
+  const int im = mat_id[e] - 1;
+  const double E = ym[im], v = nu[im];
+  const double onepv = 1.0 + v, onemv = 1.0 - v, onem2v = 1.0 - 2.0 * v;
+  const double Ef = E / (onepv * onem2v);
+  const double w1[3] = {1.0 / 3.0, 4.0 / 3.0, 1.0 / 3.0};
+  const double* g = geo + ((size_t)e * NGLL + q) * GEO_STRIDE;
+  const double wd = w1[q % 3] * w1[(q / 3) % 3] * w1[q / 9] * g[9];
+  float* r = rec + ((size_t)le * NGLL + q) * REC;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) r[i] = (float)g[i];
+  r[9] = (float)(wd * onemv * Ef);
+  r[10] = (float)(wd * v * Ef);
+  r[11] = (float)(wd * 0.5 * onem2v * Ef);
+}
+
+}  // namespace mf
+
+template <int KR>
+void launch_apply_mf(const float* rec, const int* ge, int nelmt, const float* pold, const float* z, int combine,
+                     float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, cudaStream_t s) {
+  using S = mf::Shape<KR>;
+  const int nb = (nelmt + S::EPC - 1) / S::EPC;
+  const int grid = nb < 152 * 8 ? nb : 152 * 8;
+  if (grid < 1) return;
+  mf::k_apply_mf<KR><<<grid, S::NT, 0, s>>>(rec, ge, nelmt, pold, z, combine, Y, cs, G, pos);
+}
+
+void launch_mf_record(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
+                      const double* nu, float* rec, cudaStream_t s) {
+  if (nel <= 0 || !rec) return;
+  const int n = nel * NGLL;
+  mf::k_mf_record<<<(n + 255) / 256, 256, 0, s>>>(geo, mat_id, elist, nel, ym, nu, rec);
+}
+
+template void launch_apply_mf<1>(const float*, const int*, int, const float*, const float*, int, float*,
+                                 const ColState*, const PcgGlobal*, const int*, cudaStream_t);
+template void launch_apply_mf<2>(const float*, const int*, int, const float*, const float*, int, float*,
+                                 const ColState*, const PcgGlobal*, const int*, cudaStream_t);
+template void launch_apply_mf<4>(const float*, const int*, int, const float*, const float*, int, float*,
+                                 const ColState*, const PcgGlobal*, const int*, cudaStream_t);
+template void launch_apply_mf<8>(const float*, const int*, int, const float*, const float*, int, float*,
+                                 const ColState*, const PcgGlobal*, const int*, cudaStream_t);
+template void launch_apply_mf<16>(const float*, const int*, int, const float*, const float*, int, float*,
+                                  const ColState*, const PcgGlobal*, const int*, cudaStream_t);
+
+}  // namespace sg

@@ -394,9 +394,11 @@ void launch_expand_dense(const double* Ks64, int nel, double* dense, const int* 
 constexpr int APPLY_WARPS = 4;
 // 0 = register-staged loads, 1 = TMA bulk-copy pipeline (node lanes),
 // 2 = tensor cores (FP32, 8/16 RHS), 3 = lane per (element, RHS) for FP32
-// with 8/16 RHS and the TMA node-lane pipeline otherwise (default)
+// with 8/16 RHS and the TMA node-lane pipeline otherwise (default),
+// 4 = as 3 for FP64, matrix-free for the FP32 operator of the mixed solve
 int g_apply_variant = 3;
 void set_apply_variant(int v) { g_apply_variant = v; }
+bool fp32_matrix_free() { return g_apply_variant == 4; }
 // device copy of the stored-entry table, needed by the tensor-core apply
 const int* g_entry_dev = nullptr;
 void set_entry_table(const int* d_entry) { g_entry_dev = d_entry; }
@@ -718,6 +720,11 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
                const ColState* cs, const PcgGlobal* G, const int* d_nbr, const int* pos, cudaStream_t s) {
   if (nelmt <= 0) return;
   int blocks = (nelmt + APPLY_WARPS - 1) / APPLY_WARPS;
+  if (dense == 2) {
+    if constexpr (std::is_same<V, float>::value)
+      SG_LAUNCH launch_apply_mf<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, pos, s);
+    return;
+  }
   if (dense) {
     if constexpr (std::is_same<V, double>::value && KR == 1)
       SG_LAUNCH k_apply_dense64<<<blocks, APPLY_WARPS * 32, 0, s>>>((const double*)K, ge, nelmt, p_old, z, combine, Y, cs, G,

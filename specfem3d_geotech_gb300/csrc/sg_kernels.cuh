@@ -54,6 +54,15 @@ template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
                         float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, cudaStream_t s);
 int apply_lanes_error_flag(cudaStream_t s);
+// Matrix-free FP32 apply (sg_apply_mf.cu): rec holds per GLL point J^-1 and the
+// C constants times w detJ; pcg_apply takes it with dense = 2.
+template <int KR>
+void launch_apply_mf(const float* rec, const int* ge, int nelmt, const float* pold, const float* z, int combine,
+                     float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, cudaStream_t s);
+void launch_mf_record(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
+                      const double* nu, float* rec, cudaStream_t s);
+constexpr int MF_REC = 12;        // floats per GLL point of the matrix-free record
+bool fp32_matrix_free();          // the FP32 operator of the mixed solve is applied matrix-free
 void set_gather_variant(int v);  // 1 row-cooperative gather for FP32 with 4/8/16 RHS (default), 0 staged
 template <typename V, int KR>
 // Y receives element slot (e, a)'s three rows (x KR) at the slot's gather

@@ -356,3 +356,19 @@ def test_mixed_batch_of_eight_equals_single_trials(ctx, slope):
         (r1,), x1 = m.trials([srfs[t]], ctl, want_x=True)
         assert res[t]["nl_iter"] == r1["nl_iter"]
         assert rel(xb[t], x1[0]) <= MIXED_TOL
+
+
+@pytest.mark.parametrize("k", [1, 8, 16])
+def test_matrix_free_fp32_operator_matches_stored(tmp_path, k):
+    """The matrix-free FP32 operator (stress fluxes at the GLL points from
+    J^-1 and C, no stored element matrix) drives the mixed solve to the same
+    trials as the stored FP32 matrices, to the mixed-precision tolerance, with
+    the same plastic-iteration counts; two runs of it are bitwise equal."""
+    srfs = [1.0 + 0.025 * t for t in range(k)]
+    a = _variant_trials(3, srfs, tmp_path / "st.npz")
+    b = _variant_trials(4, srfs, tmp_path / "mf.npz")
+    c = _variant_trials(4, srfs, tmp_path / "mf2.npz")
+    assert a["nl"].tolist() == b["nl"].tolist()
+    for t in range(k):
+        assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
+    assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
