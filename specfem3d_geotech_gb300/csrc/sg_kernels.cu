@@ -631,8 +631,9 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
 #pragma unroll
         for (int j = 0; j < KR; ++j) acc[c][j] = (V)0;
       const int* tb = nbr + lane * KS_NBR;
-      if constexpr (std::is_same<V, float>::value && KR % 2 == 0) {
-        // packed FP32x2 FMAs: two right-hand sides per instruction
+      if constexpr (std::is_same<V, float>::value && KR % 4 == 0) {
+        // packed FP32x2 FMAs: two right-hand sides per instruction (p rows
+        // are read as 16-byte vectors, so KR must be a multiple of 4)
         float2 acc2[3][KR / 2];
 #pragma unroll
         for (int c = 0; c < 3; ++c)

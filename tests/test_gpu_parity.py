@@ -358,7 +358,7 @@ def test_mixed_batch_of_eight_equals_single_trials(ctx, slope):
         assert rel(xb[t], x1[0]) <= MIXED_TOL
 
 
-@pytest.mark.parametrize("k", [1, 8, 16])
+@pytest.mark.parametrize("k", [1, 2, 8, 16])
 def test_matrix_free_fp32_operator_matches_stored(tmp_path, k):
     """The matrix-free FP32 operator (stress fluxes at the GLL points from
     J^-1 and C, no stored element matrix) drives the mixed solve to the same
