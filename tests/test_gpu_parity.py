@@ -363,8 +363,10 @@ def test_matrix_free_fp32_operator_matches_stored(tmp_path, k):
     """The matrix-free FP32 operator (stress fluxes at the GLL points from
     J^-1 and C, no stored element matrix) drives the mixed solve to the same
     trials as the stored FP32 matrices, to the mixed-precision tolerance, with
-    the same plastic-iteration counts; two runs of it are bitwise equal."""
-    srfs = [1.0 + 0.025 * t for t in range(k)]
+    the same plastic-iteration counts; two runs of it are bitwise equal.  All
+    probes stay below the critical SRF 1.35 (a failing trial's displacement
+    grows without bound and is not comparable)."""
+    srfs = [1.0 + 0.02 * t for t in range(k)]
     a = _variant_trials(3, srfs, tmp_path / "st.npz")
     b = _variant_trials(4, srfs, tmp_path / "mf.npz")
     c = _variant_trials(4, srfs, tmp_path / "mf2.npz")
