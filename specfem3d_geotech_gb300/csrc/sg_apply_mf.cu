@@ -83,30 +83,47 @@ __global__ void __launch_bounds__(Shape<KR>::NT) k_apply_mf(
   const float beta = (act && combine) ? (float)cs[j].beta : 0.f;
   float* U = sU[act ? el : 0];
   float* F = sS[act ? el : 0];
-  for (int e0 = blockIdx.x * S::EPC; e0 < nelmt; e0 += gridDim.x * S::EPC) {
-    const int e = e0 + el;
+  const int estride = gridDim.x * S::EPC;
+  // software pipeline: the next element's dof numbers arrive during this
+  // element's first phase and its p and z values during the second, so the
+  // global-memory latency overlaps the shared-memory arithmetic
+  auto load_dofs = [&](int e, int (&gd)[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gd[c] = (act && e < nelmt) ? __ldg(ge + (size_t)e * NEDOF + 3 * a + c) : 0;
+  };
+  auto load_p = [&](const int (&gd)[3], float (&pv)[3], float (&zv)[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      pv[c] = pold[(size_t)gd[c] * KR + j];
+      zv[c] = combine ? z[(size_t)gd[c] * KR + j] : 0.f;
+    }
+  };
+  int e = blockIdx.x * S::EPC + el;
+  int gd[3];
+  float pv[3], zv[3];
+  load_dofs(e, gd);
+  load_p(gd, pv, zv);
+  for (int e0 = blockIdx.x * S::EPC; e0 < nelmt; e0 += estride, e += estride) {
     const bool valid = act && e < nelmt;
     if (act) {
-      float u[3] = {0.f, 0.f, 0.f};
-      if (valid) {
-        const int* g = ge + (size_t)e * NEDOF + 3 * a;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const int gd = __ldg(g + c);
-          float pv = pold[(size_t)gd * KR + j];
-          if (combine) pv = fmaf(beta, pv, z[(size_t)gd * KR + j]);
-          u[c] = pv;
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < 3; ++c) U[(3 * a + c) * KR + j] = u[c];
+      for (int c = 0; c < 3; ++c) U[(3 * a + c) * KR + j] = valid ? (combine ? fmaf(beta, pv[c], zv[c]) : pv[c]) : 0.f;
+    }
+    int gdn[3];
+    load_dofs(e + estride, gdn);
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
+    int q = -1;
+    if (valid) {
+      const float4* R = reinterpret_cast<const float4*>(rec + ((size_t)e * NGLL + a) * REC);
+      r0 = __ldg(R);
+      r1 = __ldg(R + 1);
+      r2 = __ldg(R + 2);
+      q = __ldg(pos + (size_t)e * NGLL + a);
     }
     __syncthreads();
     if (valid) {
       float gr[3][3];
       ref_grad<KR>(U, a, j, gr);
-      const float4* R = reinterpret_cast<const float4*>(rec + ((size_t)e * NGLL + a) * REC);
-      const float4 r0 = __ldg(R), r1 = __ldg(R + 1), r2 = __ldg(R + 2);
       const float Ji[9] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x};
       const float c11 = r2.y, c12 = r2.z, c44 = r2.w;
       // physical gradient gp[c][d] = du_c/dx_d = sum_r Ji[3d+r] gr[c][r]
@@ -133,6 +150,7 @@ __global__ void __launch_bounds__(Shape<KR>::NT) k_apply_mf(
           F[((3 * a + c) * 3 + r) * KR + j] =
               fmaf(Ji[r], T[c][0], fmaf(Ji[3 + r], T[c][1], Ji[6 + r] * T[c][2]));
     }
+    load_p(gdn, pv, zv);
     __syncthreads();
     if (valid) {
       // rows of node a: y_c(a) = sum_r sum_t D[t][i_r(a)] F_(point t on line r)[c][r]
@@ -151,7 +169,6 @@ __global__ void __launch_bounds__(Shape<KR>::NT) k_apply_mf(
           y2 = fmaf(d, f[6 * KR], y2);
         }
       }
-      const int q = pos[(size_t)e * NGLL + a];
       if (q >= 0) {
         float* dst = Y + (size_t)q * 3 * KR + j;
         dst[0] = y0;
