@@ -86,65 +86,28 @@ __global__ void __launch_bounds__(Shape<KR>::NT) k_apply_mf(
   const int estride = gridDim.x * S::EPC;
   // software pipeline: the next element's dof numbers arrive during this
   // element's first phase and its p and z values during the second, so the
-  // global-memory latency overlaps the shared-memory arithmetic.  With KR a
-  // multiple of 4 a node's three dof rows are read as 3 KR / 4 pieces of 16
-  // bytes by as many of its lanes (piece q: dof q / (KR/4), columns
-  // 4 (q mod KR/4) ..+3); otherwise each lane reads its own column.
-  constexpr bool VEC = (KR % 4) == 0;
-  constexpr int QPD = VEC ? KR / 4 : 1;
-  const int pc = VEC ? j / QPD : 0, pcol = VEC ? 4 * (j - pc * QPD) : j;
-  const bool ploader = act && (!VEC || j < 3 * QPD);
-  float betas[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) betas[k] = (VEC && ploader && combine) ? (float)cs[pcol + k].beta : beta;
+  // global-memory latency overlaps the shared-memory arithmetic
   auto load_dofs = [&](int e, int (&gd)[3]) {
-    if constexpr (VEC) {
-      gd[0] = (ploader && e < nelmt) ? __ldg(ge + (size_t)e * NEDOF + 3 * a + pc) : 0;
-    } else {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) gd[c] = (act && e < nelmt) ? __ldg(ge + (size_t)e * NEDOF + 3 * a + c) : 0;
-    }
+    for (int c = 0; c < 3; ++c) gd[c] = (act && e < nelmt) ? __ldg(ge + (size_t)e * NEDOF + 3 * a + c) : 0;
   };
-  auto load_p = [&](const int (&gd)[3], float4 (&pv)[3], float4 (&zv)[3]) {
-    if constexpr (VEC) {
-      if (ploader) {
-        pv[0] = *reinterpret_cast<const float4*>(pold + (size_t)gd[0] * KR + pcol);
-        zv[0] = combine ? *reinterpret_cast<const float4*>(z + (size_t)gd[0] * KR + pcol) : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-    } else {
+  auto load_p = [&](const int (&gd)[3], float (&pv)[3], float (&zv)[3]) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        pv[c].x = pold[(size_t)gd[c] * KR + j];
-        zv[c].x = combine ? z[(size_t)gd[c] * KR + j] : 0.f;
-      }
+    for (int c = 0; c < 3; ++c) {
+      pv[c] = pold[(size_t)gd[c] * KR + j];
+      zv[c] = combine ? z[(size_t)gd[c] * KR + j] : 0.f;
     }
   };
   int e = blockIdx.x * S::EPC + el;
-  int gd[3] = {0, 0, 0};
-  float4 pv[3], zv[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) pv[c] = zv[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+  int gd[3];
+  float pv[3], zv[3];
   load_dofs(e, gd);
   load_p(gd, pv, zv);
   for (int e0 = blockIdx.x * S::EPC; e0 < nelmt; e0 += estride, e += estride) {
     const bool valid = act && e < nelmt;
-    if constexpr (VEC) {
-      if (ploader) {
-        float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (valid) {
-          u.x = combine ? fmaf(betas[0], pv[0].x, zv[0].x) : pv[0].x;
-          u.y = combine ? fmaf(betas[1], pv[0].y, zv[0].y) : pv[0].y;
-          u.z = combine ? fmaf(betas[2], pv[0].z, zv[0].z) : pv[0].z;
-          u.w = combine ? fmaf(betas[3], pv[0].w, zv[0].w) : pv[0].w;
-        }
-        *reinterpret_cast<float4*>(U + (3 * a + pc) * KR + pcol) = u;
-      }
-    } else {
-      if (act) {
+    if (act) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
-          U[(3 * a + c) * KR + j] = valid ? (combine ? fmaf(beta, pv[c].x, zv[c].x) : pv[c].x) : 0.f;
-      }
+      for (int c = 0; c < 3; ++c) U[(3 * a + c) * KR + j] = valid ? (combine ? fmaf(beta, pv[c], zv[c]) : pv[c]) : 0.f;
     }
     int gdn[3];
     load_dofs(e + estride, gdn);
