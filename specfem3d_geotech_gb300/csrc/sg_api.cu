@@ -9,7 +9,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <array>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -72,6 +74,48 @@ struct sg_ctx {
     ColState* cs = nullptr;
     PcgGlobal* G = nullptr;
   } dropin;
+
+  // CUDA graphs of PCG iteration chunks on small meshes, where launching
+  // three short kernels per iteration from the host costs as much as running
+  // them.  Keyed by every argument of the captured launches; a chunk replays
+  // exactly the kernels (and arguments) the eager loop would launch.
+  struct ChunkGraph {
+    std::array<uintptr_t, 26> key{};
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::vector<ChunkGraph> graphs;
+  bool graphs_ok = true;
+  cudaGraphExec_t chunk_graph(const std::array<uintptr_t, 26>& key, const std::function<void()>& launch) {
+    for (auto& g : graphs)
+      if (g.key == key) return g.exec;
+    if (!graphs_ok) return nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      graphs_ok = false;
+      return nullptr;
+    }
+    launch();
+    const cudaError_t e1 = cudaStreamEndCapture(stream, &graph);
+    const cudaError_t e2 = (e1 == cudaSuccess) ? cudaGraphInstantiate(&exec, graph, 0) : e1;
+    if (graph) cudaGraphDestroy(graph);
+    if (e2 != cudaSuccess) {
+      cudaGetLastError();
+      graphs_ok = false;  // eager launches from now on
+      return nullptr;
+    }
+    if (graphs.size() >= 16) {
+      cudaGraphExecDestroy(graphs.front().exec);
+      graphs.erase(graphs.begin());
+    }
+    graphs.push_back({key, exec});
+    return exec;
+  }
+  void drop_graphs() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+  }
 
   bool check(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return true;
@@ -199,7 +243,7 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
   int it = 0;
   int status = SG_OK;
   volatile PcgGlobal* hG = (volatile PcgGlobal*)C->pin;
-  while (true) {
+  auto eager_chunk = [&]() {
     for (int c = 0; c < chunk; ++c) {
       ev = C->prof_begin();
       pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, B.p, B.z, 1, B.Y, B.cs, B.G, C->d_nbr, op.T->d_pos, s);
@@ -211,6 +255,27 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
       pcg_update<V, KR>(n1, u, B.r, B.z, B.p, B.kp, f, dp, 0, B.cs, B.G, B.part, s);
       C->prof_end(ev, 3);
     }
+  };
+  // small meshes replay the chunk as a CUDA graph after one eager chunk (which
+  // also sets every kernel attribute outside any capture); profiling keeps
+  // the eager loop so that each launch is bracketed by its events
+  const bool graphs = !C->prof.on && op.nelmt < 20000;
+  const std::array<uintptr_t, 26> key = {
+      (uintptr_t)op.dense, (uintptr_t)op.K, (uintptr_t)op.ge, (uintptr_t)op.nelmt, (uintptr_t)op.T->d_ptr,
+      (uintptr_t)op.T->d_ent, (uintptr_t)op.T->d_dof, (uintptr_t)op.T->d_pos, (uintptr_t)op.T->ngroups,
+      (uintptr_t)C->d_nbr, (uintptr_t)B.Y, (uintptr_t)B.kp, (uintptr_t)B.p, (uintptr_t)B.z, (uintptr_t)B.r,
+      (uintptr_t)B.cs, (uintptr_t)B.G, (uintptr_t)B.part, (uintptr_t)u, (uintptr_t)f, (uintptr_t)dp,
+      (uintptr_t)n1, (uintptr_t)KR, (uintptr_t)sizeof(V), (uintptr_t)chunk, (uintptr_t)0};
+  int nchunks = 0;
+  while (true) {
+    cudaGraphExec_t ex = (graphs && nchunks > 0) ? C->chunk_graph(key, eager_chunk) : nullptr;
+    if (ex) {
+      cudaGraphLaunch(ex, s);
+      add_launches(3LL * chunk);
+    } else {
+      eager_chunk();
+    }
+    ++nchunks;
     cudaMemcpyAsync((void*)hG, B.G, sizeof(PcgGlobal), cudaMemcpyDeviceToHost, s);
     if (!C->check(cudaStreamSynchronize(s), "pcg")) return SG_ERR_CUDA;
     it = hG->it;
@@ -333,6 +398,7 @@ void sg_destroy(sg_ctx* c) {
   cudaStreamSynchronize(c->stream);
   for (auto& kv : c->live) cudaFree(kv.first);
   c->live.clear();
+  c->drop_graphs();
   for (auto& e : c->ev_pool) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   for (auto& e : c->marks) if (e) cudaEventDestroy(e);
   if (c->pin) cudaFreeHost(c->pin);
@@ -708,6 +774,7 @@ void sg_model_free(sg_model* M) {
   if (!M) return;
   sg_ctx* c = M->ctx;
   cudaStreamSynchronize(c->stream);
+  c->drop_graphs();  // captured chunks may name this model's buffers
   model_release_work(M);
   free_topo(c, M->T);
   for (void* p : {(void*)M->d_coord, (void*)M->d_gnum, (void*)M->d_matid, (void*)M->d_ge, (void*)M->d_gdof,

@@ -28,6 +28,7 @@ namespace sg {
 // host-side count of kernel launches issued by this library
 std::atomic<long long> g_launch_count{0};
 long long launch_count() { return g_launch_count.load(); }
+void add_launches(long long n) { g_launch_count += n; }
 #define SG_LAUNCH ++g_launch_count,
 
 // D[p][m] = derivative of the m-th 1D Lagrange polynomial on the GLL points

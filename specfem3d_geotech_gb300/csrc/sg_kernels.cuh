@@ -41,6 +41,7 @@ struct MatF {
 
 // Kernel launch wrappers (sg_kernels.cu)
 long long launch_count();        // kernel launches issued so far (host counter)
+void add_launches(long long n);  // kernels launched through a replayed CUDA graph
 void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline, 2 tensor cores for 8/16 FP32 RHS,
                                  // 3 lane per (element, RHS) for 8/16 FP32 RHS
 void set_entry_table(const int* d_entry);
