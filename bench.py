@@ -220,11 +220,13 @@ def run_reference(args, rank, world):
     return 0
 
 
-def apply_kernel_name(kr: int) -> str:
-    v = os.environ.get("SG_APPLY_VARIANT", "3")
+def apply_kernel_name(kr: int, nelmt: int) -> str:
+    v = os.environ.get("SG_APPLY_VARIANT", "5")
     if v == "2" and kr in (8, 16):
         return f"k_apply_tc<{kr}>"
-    if v == "3" and kr in (8, 16):
+    if v == "4" or (v == "5" and nelmt < 100000):
+        return f"k_apply_mf<{kr}>"
+    if v in ("3", "5") and kr in (8, 16):
         return f"k_apply_lanes<{kr}>"
     return f"k_apply_sparse_tma<float,{kr}>"
 
@@ -435,7 +437,7 @@ def run_ours(args, rank, world, local):
                        "mixed_batched_over_plain": rate_all / rate64 if rate64 == rate64 else None},
         "precision": precision,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "kernel": apply_kernel_name(kr),
+                     "traffic": traffic, "kernel": apply_kernel_name(kr, ne),
                      "algorithmic_bytes_per_launch": bytes_apply, "avg_launch_ms": apply_ms,
                      "peak_source": peak_kind},
         "kernel_ms_per_pcg_iter": {"apply": apply_ms,

@@ -352,7 +352,8 @@ sg_ctx* sg_create(int device, size_t hbm_budget) {
   cudaMallocHost((void**)&c->pin, 4096);
   upload_constants();
   // SG_APPLY_VARIANT selects another element apply for cross-checking:
-  // 0 register-staged, 1 TMA node lanes, 2 tensor cores (default 3).
+  // 0 register-staged, 1 TMA node lanes, 2 tensor cores, 3 lane apply,
+  // 4 matrix-free FP32 (default 5: lane apply, matrix-free FP32 on small meshes).
   if (const char* v = std::getenv("SG_APPLY_VARIANT")) set_apply_variant(std::atoi(v));
   // SG_GATHER_VARIANT=0 selects the shared-memory-staged gather everywhere.
   if (const char* v = std::getenv("SG_GATHER_VARIANT")) set_gather_variant(std::atoi(v));
@@ -916,7 +917,7 @@ struct SolveStats {
 static Op fp32_op(const sg_model* M, const Op& op64) {
   Op o = op64;
   o.K = M->d_K32;
-  if (fp32_matrix_free()) {
+  if (fp32_matrix_free(op64.nelmt)) {
     o.dense = 2;
     o.K = M->d_rec32;
   }

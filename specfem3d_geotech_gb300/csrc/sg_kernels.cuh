@@ -43,7 +43,8 @@ struct MatF {
 long long launch_count();        // kernel launches issued so far (host counter)
 void add_launches(long long n);  // kernels launched through a replayed CUDA graph
 void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline, 2 tensor cores for 8/16 FP32 RHS,
-                                 // 3 lane per (element, RHS) for 8/16 FP32 RHS
+                                 // 3 lane per (element, RHS) for 8/16 FP32 RHS, 4 matrix-free FP32,
+                                 // 5 (default) 3 with matrix-free FP32 on small meshes
 void set_entry_table(const int* d_entry);
 int apply_tc_error_flag(cudaStream_t s);
 template <int KR>
@@ -63,7 +64,7 @@ void launch_apply_mf(const float* rec, const int* ge, int nelmt, const float* po
 void launch_mf_record(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
                       const double* nu, float* rec, cudaStream_t s);
 constexpr int MF_REC = 12;        // floats per GLL point of the matrix-free record
-bool fp32_matrix_free();          // the FP32 operator of the mixed solve is applied matrix-free
+bool fp32_matrix_free(int nelmt);  // the FP32 operator of the mixed solve is applied matrix-free
 void set_gather_variant(int v);  // 1 row-cooperative gather for FP32 with 4/8/16 RHS (default), 0 staged
 template <typename V, int KR>
 // Y receives element slot (e, a)'s three rows (x KR) at the slot's gather

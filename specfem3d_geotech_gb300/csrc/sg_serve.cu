@@ -40,12 +40,14 @@ struct Request {
 
 // Device bytes of a request's model and an SRF batch of KR slots, per element
 // (about 25 dofs per element on 27-node meshes): FP64 and FP32 element matrices,
-// geometry, per-slot plastic state, element products and vectors.
+// the matrix-free point records, geometry, per-slot plastic state, element
+// products and vectors.
 size_t estimate_footprint(int nelmt, int k, int precision) {
   const size_t kr = (size_t)(1 << (int)std::ceil(std::log2(std::max(1, k))));
   const size_t ne = (size_t)nelmt, neq = 26 * ne;
   size_t b = ne * sg::KS_STRIDE * 8 + ne * 27 * 10 * 8 + ne * 81 * 8 * 2;
-  if (precision == SG_PREC_MIXED) b += ne * sg::KS_STRIDE * 4 + ne * 81 * kr * 4 + neq * kr * 4 * 6;
+  if (precision == SG_PREC_MIXED)
+    b += ne * sg::KS_STRIDE * 4 + ne * sg::NGLL * sg::MF_REC * 4 + ne * 81 * kr * 4 + neq * kr * 4 * 6;
   b += kr * ne * 27 * 6 * 8 * 2 + ne * 81 * kr * 8 + neq * kr * 8 * 8 + ne * 27 * 4 * 2;
   return b + (b >> 3) + (size_t(64) << 20);
 }
