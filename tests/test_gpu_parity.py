@@ -374,3 +374,21 @@ def test_matrix_free_fp32_operator_matches_stored(tmp_path, k):
     for t in range(k):
         assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
     assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
+
+
+def test_graph_replay_bitwise_equal_to_eager(ctx, slope):
+    """On small meshes each chunk of PCG iterations is replayed as a captured
+    CUDA graph; with profiling on the same chunk runs as eager launches.  Both
+    give bitwise the same trial (the graph holds exactly the eager launches)."""
+    mesh, _ = slope
+    m = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    ctl = sg.make_control(precision=sg.PREC_MIXED)
+    srfs = [1.0, 1.1, 1.2]
+    r_graph, x_graph = m.trials(srfs, ctl, want_x=True)
+    ctx.profile(True)
+    try:
+        r_eager, x_eager = m.trials(srfs, ctl, want_x=True)
+    finally:
+        ctx.profile(False)
+    assert np.array_equal(x_graph, x_eager)
+    assert [r["cg_tot"] for r in r_graph] == [r["cg_tot"] for r in r_eager]
