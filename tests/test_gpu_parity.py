@@ -392,3 +392,18 @@ def test_graph_replay_bitwise_equal_to_eager(ctx, slope):
         ctx.profile(False)
     assert np.array_equal(x_graph, x_eager)
     assert [r["cg_tot"] for r in r_graph] == [r["cg_tot"] for r in r_eager]
+
+
+@pytest.mark.parametrize("k", [1, 8, 16])
+def test_matrix_free_line_form_bitwise_equals_point_form(tmp_path, k):
+    """The line form of the matrix-free apply (xi terms kept in registers)
+    does the point form's arithmetic in the same order: bitwise equal trials."""
+    srfs = [1.0 + 0.02 * t for t in range(k)]
+    os.environ.pop("SG_MF_POINTS", None)
+    a = _variant_trials(4, srfs, tmp_path / "lines.npz")
+    try:
+        os.environ["SG_MF_POINTS"] = "1"
+        b = _variant_trials(4, srfs, tmp_path / "points.npz")
+    finally:
+        os.environ.pop("SG_MF_POINTS", None)
+    assert np.array_equal(a["x"], b["x"]) and np.array_equal(a["cg"], b["cg"])
