@@ -916,12 +916,12 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather(
 // equal to it; the p.kp partials are compensated sums over the lane's four
 // columns, reduced in a fixed order.
 int g_gather_variant = 1;   // 0 = staged gather for every case
-constexpr int GATHER_ROWS_BLOCKS = 152 * 5;
+constexpr int GATHER_ROWS_BLOCKS = 152 * 4;   // one wave: four resident CTAs per SM at 64 registers
 static_assert(GATHER_ROWS_BLOCKS * 16 <= NPART * 16 * 4, "p.kp partials fit the partial buffer");
 void set_gather_variant(int v) { g_gather_variant = v; }
 
 template <int KR>
-__global__ void __launch_bounds__(RED_THREADS) k_pcg_gather_rows(
+__global__ void __launch_bounds__(RED_THREADS, 4) k_pcg_gather_rows(
     const int* __restrict__ ptr, const int* __restrict__ dof, int ng, const float* __restrict__ Y,
     float* __restrict__ kp, float* __restrict__ p, const float* __restrict__ z, int mode, ColState* __restrict__ cs,
     PcgGlobal* __restrict__ G, double* __restrict__ part) {
@@ -949,13 +949,34 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather_rows(
     if (!act || g >= ng) continue;
     const int a = ptr[g], b = ptr[g + 1];
     const int gd = dof[3 * g + d];
+    // the p and z rows do not depend on the sums: their loads go out with the
+    // first slot loads (two dependent trips per node instead of three)
+    float4* pp = reinterpret_cast<float4*>(p + (size_t)gd * KR + c0);
+    float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), zv = pv;
+    if (mode != 0 && gd) {
+      pv = *pp;
+      zv = *reinterpret_cast<const float4*>(z + (size_t)gd * KR + c0);
+    }
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int sl = a; sl < b; ++sl) {
-      const float4 v = __ldcs(yq + (size_t)sl * LPN);
-      acc.x = acc.x + v.x;
-      acc.y = acc.y + v.y;
-      acc.z = acc.z + v.z;
-      acc.w = acc.w + v.w;
+    // up to four slots in flight at once, summed in slot order
+    float4 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (a + k < b) v[k] = __ldcs(yq + (size_t)(a + k) * LPN);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (a + k < b) {
+        acc.x = acc.x + v[k].x;
+        acc.y = acc.y + v[k].y;
+        acc.z = acc.z + v[k].z;
+        acc.w = acc.w + v[k].w;
+      }
+    for (int sl = a + 4; sl < b; ++sl) {
+      const float4 w = __ldcs(yq + (size_t)sl * LPN);
+      acc.x = acc.x + w.x;
+      acc.y = acc.y + w.y;
+      acc.z = acc.z + w.z;
+      acc.w = acc.w + w.w;
     }
     if (!gd) continue;
     float4* kpo = reinterpret_cast<float4*>(kp + (size_t)gd * KR + c0);
@@ -963,9 +984,6 @@ __global__ void __launch_bounds__(RED_THREADS) k_pcg_gather_rows(
       *kpo = acc;
       continue;
     }
-    float4* pp = reinterpret_cast<float4*>(p + (size_t)gd * KR + c0);
-    float4 pv = *pp;
-    const float4 zv = *reinterpret_cast<const float4*>(z + (size_t)gd * KR + c0);
     if (live[0]) { pv.x = pdir(beta[0], pv.x, zv.x); dacc[0].add(pv.x, acc.x); }
     if (live[1]) { pv.y = pdir(beta[1], pv.y, zv.y); dacc[1].add(pv.y, acc.y); }
     if (live[2]) { pv.z = pdir(beta[2], pv.z, zv.z); dacc[2].add(pv.z, acc.z); }
@@ -1012,8 +1030,7 @@ void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mo
                 double* part, cudaStream_t s) {
   if constexpr (std::is_same<V, float>::value && (KR == 4 || KR == 8 || KR == 16)) {
     if (g_gather_variant == 1) {
-      // five resident CTAs per SM (register-limited), one wave: measured
-      // 0.244 ms against 0.279 ms with four per SM on the 192k-element slope
+      // one wave of resident CTAs (the grid depends only on the problem size)
       constexpr int NPB = GATHER_WARPS * (32 / (3 * KR / 4));   // nodes per block and pass
       SG_LAUNCH k_pcg_gather_rows<KR><<<red_grid(T.ngroups, NPB * 4, GATHER_ROWS_BLOCKS), RED_THREADS, 0, s>>>(T.d_ptr, T.d_dof, T.ngroups, Y, kp, p, z, mode,
                                                                    cs, G, part);
