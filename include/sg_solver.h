@@ -116,6 +116,12 @@ int sg_model_control(const sg_model* model, double* dctl, int* ictl, double* srf
  * dprecon (0:neq, before inversion) and gravity load extload (0:neq) as built on
  * the device by stiffness_bodyload; any pointer may be NULL. */
 int sg_model_stiffness(sg_model* model, double* storekm, double* dprecon, double* extload);
+/* Pseudo-static earthquake load (the deck's eqload: line, src/read_input.f90:293-303,
+ * applied as in src/preprocess.f90:137-143): every later slope trial's external
+ * load gains eqk * gamma * w detJ per node and direction on top of gravity.  The
+ * excavation driver keeps gravity alone (src/excavation.F90:191).  Rebuilds the
+ * stiffness and loads; SG_ERR_BADARG while a trial batch is open. */
+int sg_model_set_eqload(sg_model* model, double eqkx, double eqky, double eqkz);
 
 /* ---- one strength-reduction trial of slope3d (src/slope.F90:244-443) ---- */
 typedef struct sg_control {

@@ -45,6 +45,7 @@ def lib():
         L.orc_model_control.argtypes = [vp, _dp, _ip, vp]
         L.orc_set_control.argtypes = [vp, d, i, d, i, i, i]
         L.orc_stiffness_bodyload.argtypes = [vp, _dp, _dp, _dp]
+        L.orc_set_eqload.argtypes = [vp, d, d, d]
         L.orc_pcg_solver.restype = i
         L.orc_pcg_solver.argtypes = [i, i, _dp, _dp, _dp, _dp, _ip, i, d, C.POINTER(C.c_int)]
         L.orc_ebe_apply.argtypes = [i, i, _dp, _dp, _ip, _dp]
@@ -105,6 +106,10 @@ class OracleModel:
         if getattr(self, "h", None):
             lib().orc_free(self.h)
             self.h = None
+
+    def set_eqload(self, eqkx, eqky, eqkz):
+        """Pseudo-static earthquake load factors (src/preprocess.f90:137-143)."""
+        lib().orc_set_eqload(self.h, eqkx, eqky, eqkz)
 
     def set_control(self, cg_tol, cg_maxiter, nl_tol, nl_maxiter, phinu=0, allelastic=0):
         lib().orc_set_control(self.h, cg_tol, cg_maxiter, nl_tol, nl_maxiter, phinu, allelastic)

@@ -1092,6 +1092,13 @@ void* orc_model_from_deck(const char* path) {
     for (int i = 0; i < nsrf; ++i) ss >> h->srf_list[i];
   }
   if (D.lines["material:"].count("allelastic")) C.allelastic = std::atoi(D.lines["material:"]["allelastic"].c_str()) == 1;
+  if (D.lines.count("eqload:")) {  // src/read_input.f90:293-303
+    auto& eq = D.lines["eqload:"];
+    C.iseqload = 1;
+    C.eqkx = eq.count("eqkx") ? std::atof(eq["eqkx"].c_str()) : 0.0;
+    C.eqky = eq.count("eqky") ? std::atof(eq["eqky"].c_str()) : 0.0;
+    C.eqkz = eq.count("eqkz") ? std::atof(eq["eqkz"].c_str()) : 0.0;
+  }
   return h;
 }
 
@@ -1129,8 +1136,15 @@ void orc_set_control(void* hv, double cg_tol, int cg_maxiter, double nl_tol, int
 // Element stiffness, diagonal and gravity load over all elements.
 void orc_stiffness_bodyload(void* hv, double* storekm, double* dprecon, double* extload) {
   OrcModel* h = (OrcModel*)hv;
-  stiffness_bodyload(h->M, nullptr, h->M.nelmt, h->M.nu.data(), storekm, dprecon, extload, true, false, 0, 0, 0,
-                     h->M.gdof_elmt.data());
+  stiffness_bodyload(h->M, nullptr, h->M.nelmt, h->M.nu.data(), storekm, dprecon, extload, true,
+                     h->C.iseqload != 0, h->C.eqkx, h->C.eqky, h->C.eqkz, h->M.gdof_elmt.data());
+}
+
+// Pseudo-static earthquake load factors (the eqload: line, src/read_input.f90:293-303).
+void orc_set_eqload(void* hv, double eqkx, double eqky, double eqkz) {
+  OrcModel* h = (OrcModel*)hv;
+  h->C.iseqload = 1;
+  h->C.eqkx = eqkx; h->C.eqky = eqky; h->C.eqkz = eqkz;
 }
 
 int orc_pcg_solver(int neq, int nelmt, const double* k, double* u, const double* f, const double* dprecon,

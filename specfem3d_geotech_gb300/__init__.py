@@ -34,7 +34,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 EXPORTED = (
     "sg_create", "sg_create_status", "sg_destroy", "sg_last_error", "sg_hbm_used", "sg_pcg_solve",
     "sg_model_from_hex8", "sg_model_from_deck", "sg_model_free", "sg_model_info", "sg_model_arrays",
-    "sg_model_control", "sg_model_stiffness", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
+    "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
     "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc",
     "sg_server_create", "sg_server_submit", "sg_server_wait", "sg_server_stats", "sg_server_destroy",
@@ -118,6 +118,8 @@ def lib(path: Optional[str] = None):
     L.sg_model_stiffness.argtypes = [vp, vp, vp, vp]
     L.sg_srf_trials.restype = i
     L.sg_srf_trials.argtypes = [vp, C.POINTER(Control), i, vp, vp, vp]
+    L.sg_model_set_eqload.restype = i
+    L.sg_model_set_eqload.argtypes = [vp, d, d, d]
     L.sg_last_stress.restype = i
     L.sg_last_stress.argtypes = [vp, i, vp]
     L.sg_srf_sweep.restype = i
@@ -337,6 +339,12 @@ class Model:
         if st:
             raise SgError(st, self.ctx.last_error)
         return (km.reshape(self.nelmt, 81, 81) if want_k else None), dp, ext
+
+    def set_eqload(self, eqkx: float, eqky: float, eqkz: float):
+        """Pseudo-static earthquake load factors (the deck's eqload: line)."""
+        st = lib().sg_model_set_eqload(self.h, eqkx, eqky, eqkz)
+        if st:
+            raise SgError(st, self.ctx.last_error)
 
     def trials(self, srf: Sequence[float], ctl: Control, want_x: bool = False):
         srf = np.ascontiguousarray(srf, np.float64)

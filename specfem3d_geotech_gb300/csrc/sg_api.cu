@@ -635,14 +635,15 @@ static bool model_work(sg_model* M, int KR, int n1, int nel) {
 // Builds K, the diagonal preconditioner and the gravity load for the
 // element list (all elements when elist is null) with Poisson ratios nuv.
 static bool model_stiffness(sg_model* M, const int* d_elist, int nel, const double* d_nuv, const GatherTopo& T,
-                            const int* d_ge_local, int n1, bool gravity) {
+                            const int* d_ge_local, int n1, bool gravity, bool pseudoeq = true) {
   sg_ctx* c = M->ctx;
   cudaStream_t s = c->stream;
   double* Ydiag = M->d_Yscratch;
   double* Ygrav = M->d_Yscratch + (size_t)M->H.nelmt * NEDOF;
   int ev = c->prof_begin();
   launch_stiffness(M->d_geo, M->d_matid, d_elist, nel, M->d_ym, d_nuv, M->d_gam, M->d_K64, M->d_K32, Ydiag,
-                   gravity ? Ygrav : nullptr, c->d_entry, T.d_pos, s);
+                   gravity ? Ygrav : nullptr, c->d_entry, T.d_pos, s, pseudoeq ? M->H.iseqload : 0, M->H.eqkx,
+                   M->H.eqky, M->H.eqkz);
   launch_mf_record(M->d_geo, M->d_matid, d_elist, nel, M->d_ym, d_nuv, M->d_rec32, s);
   c->prof_end(ev, 5);
   cudaMemsetAsync(M->d_diag, 0, sizeof(double) * n1, s);
@@ -784,6 +785,15 @@ void sg_model_free(sg_model* M) {
                   (void*)M->d_Yscratch, (void*)M->d_fpart})
     c->release(p);
   delete M;
+}
+
+int sg_model_set_eqload(sg_model* M, double eqkx, double eqky, double eqkz) {
+  if (!M || M->B.open) return SG_ERR_BADARG;
+  M->H.iseqload = 1;
+  M->H.eqkx = eqkx; M->H.eqky = eqky; M->H.eqkz = eqkz;
+  const int n1 = M->H.neq + 1;
+  if (!model_stiffness(M, nullptr, M->H.nelmt, M->d_nu, M->T, M->d_ge, n1, true)) return SG_ERR_CUDA;
+  return M->ctx->check(cudaStreamSynchronize(M->ctx->stream), "eqload") ? SG_OK : SG_ERR_CUDA;
 }
 
 int sg_model_info(const sg_model* M, int* info) {
@@ -1339,6 +1349,9 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
     sg_control c0 = *ctl;
     int KR = 1, n1 = h.neq + 1;
     if (!model_work(M, KR, n1, ne)) { status = SG_ERR_OOM; goto done; }
+    // the excavation's gravity load carries no pseudo-static part
+    // (src/excavation.F90:191); the model's own load is restored at the end
+    if (M->H.iseqload) model_stiffness(M, nullptr, ne, M->d_nu, M->T, M->d_ge, n1, true, false);
     {
       cudaMemsetAsync(M->W.x, 0, sizeof(double) * n1, s);
       cudaMemcpyAsync(M->W.load, M->d_extload, sizeof(double) * n1, cudaMemcpyDeviceToDevice, s);

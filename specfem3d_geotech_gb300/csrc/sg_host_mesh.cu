@@ -229,8 +229,8 @@ const KsTables& ks_tables() {
 
 // ---------------------------------------------------------------------------
 // .sem deck reader: the subset of src/read_input.f90:13-619 the solve path
-// uses (preinfo, mesh, bc, material, control, stress0; save/water/traction/
-// eqload lines are accepted and ignored).  File names resolve relative to the
+// uses (preinfo, mesh, bc, material, control, stress0, eqload; save/water/
+// traction lines are accepted and ignored).  File names resolve relative to the
 // deck's directory.  Defaults: cg_tol = nl_tol = 1e-12, cg_maxiter =
 // nl_maxiter = 100 (src/read_input.f90:109-110).
 // ---------------------------------------------------------------------------
@@ -401,6 +401,13 @@ bool read_deck(const char* path, HostMesh& M, std::vector<double>& x8, std::vect
     if (s0.count("z0")) M.z0 = std::atof(s0["z0"].c_str());
     if (s0.count("s0")) M.s0 = std::atof(s0["s0"].c_str());
     if (s0.count("k0")) M.k0 = std::atof(s0["k0"].c_str());
+  }
+  if (L.count("eqload:")) {  // src/read_input.f90:293-303
+    auto& eq = L["eqload:"];
+    M.iseqload = 1;
+    M.eqkx = eq.count("eqkx") ? std::atof(eq["eqkx"].c_str()) : 0.0;
+    M.eqky = eq.count("eqky") ? std::atof(eq["eqky"].c_str()) : 0.0;
+    M.eqkz = eq.count("eqkz") ? std::atof(eq["eqkz"].c_str()) : 0.0;
   }
   (void)nnode8;
   return true;

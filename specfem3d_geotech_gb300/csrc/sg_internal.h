@@ -65,6 +65,8 @@ struct HostMesh {
   std::vector<int> excavid, nexcavid;
   int s0_type = -1;
   double z0 = 0, s0 = 0, k0 = 0;
+  int iseqload = 0;                       // pseudo-static load (eqload: line)
+  double eqkx = 0, eqky = 0, eqkz = 0;
 };
 
 // host mesh construction (sg_host_mesh.cu)
@@ -94,7 +96,8 @@ void launch_geometry(const double* g_coord, const int* g_num, int nelmt, double*
 // per element, both gathered later into global vectors.
 void launch_stiffness(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
                       const double* nu, const double* gam, double* Ks64, float* Ks32, double* Ydiag,
-                      double* Ygrav, const int* d_entry, const int* pos, cudaStream_t s);
+                      double* Ygrav, const int* d_entry, const int* pos, cudaStream_t s,
+                      int pseudoeq = 0, double eqkx = 0, double eqky = 0, double eqkz = 0);
 void launch_expand_dense(const double* Ks64, int nel, double* dense, const int* d_entry, cudaStream_t s);
 
 }  // namespace sg

@@ -294,7 +294,8 @@ __global__ void __launch_bounds__(STIFF_THREADS) k_stiffness(
     const double* __restrict__ geo, const int* __restrict__ mat_id, const int* __restrict__ elist, int nel,
     const double* __restrict__ ym, const double* __restrict__ nu, const double* __restrict__ gam,
     double* __restrict__ Ks64, float* __restrict__ Ks32, double* __restrict__ Ydiag, double* __restrict__ Ygrav,
-    const int* __restrict__ entry, const int* __restrict__ pos) {
+    const int* __restrict__ entry, const int* __restrict__ pos, int pseudoeq, double eqkx, double eqky,
+    double eqkz) {
   __shared__ double sg[NGLL][NGLL][3];   // grad of node n at point i (zero off the lines)
   __shared__ double sgeo[NGLL][GEO_STRIDE];
   __shared__ double swd[NGLL];
@@ -356,16 +357,22 @@ __global__ void __launch_bounds__(STIFF_THREADS) k_stiffness(
     for (int t = threadIdx.x; t < NEDOF; t += blockDim.x) {
       int a = t / 3, d = t % 3;
       int ps = pos[(size_t)le * NGLL + a];
-      if (ps >= 0) Ygrav[(size_t)ps * 3 + d] = (d == 2) ? -(swd[a] * gam[im]) : -0.0;
+      if (ps < 0) continue;
+      double v = (d == 2) ? -(swd[a] * gam[im]) : -0.0;
+      // pseudo-static earthquake load (src/preprocess.f90:137-143):
+      // eqload = eqk * eld (eld = w detJ at the node's z entry), times gamma
+      if (pseudoeq) v = v + ((d == 0 ? eqkx : d == 1 ? eqky : eqkz) * swd[a]) * gam[im];
+      Ygrav[(size_t)ps * 3 + d] = v;
     }
 }
 
 void launch_stiffness(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
                       const double* nu, const double* gam, double* Ks64, float* Ks32, double* Ydiag,
-                      double* Ygrav, const int* d_entry, const int* pos, cudaStream_t s) {
+                      double* Ygrav, const int* d_entry, const int* pos, cudaStream_t s, int pseudoeq,
+                      double eqkx, double eqky, double eqkz) {
   if (nel <= 0) return;
   SG_LAUNCH k_stiffness<<<nel, STIFF_THREADS, 0, s>>>(geo, mat_id, elist, nel, ym, nu, gam, Ks64, Ks32, Ydiag, Ygrav,
-                                           d_entry, pos);
+                                           d_entry, pos, pseudoeq, eqkx, eqky, eqkz);
 }
 
 // Expand the sparse symmetric layout to the reference's dense column-major

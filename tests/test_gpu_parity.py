@@ -407,3 +407,29 @@ def test_matrix_free_line_form_bitwise_equals_point_form(tmp_path, k):
     finally:
         os.environ.pop("SG_MF_POINTS", None)
     assert np.array_equal(a["x"], b["x"]) and np.array_equal(a["cg"], b["cg"])
+
+
+def test_pseudo_static_load_matches_oracle(ctx, tmp_path):
+    """sg_model_set_eqload builds the load of src/preprocess.f90:137-143 (the
+    deck's eqload: line gives the same model), and a plastic trial under it
+    matches the oracle's."""
+    mesh = meshgen.slope2d()
+    om = OracleModel(mesh)
+    om.set_eqload(0.05, 0.0, 0.0)
+    _, _, ext_o = om.stiffness_bodyload()
+    m = sg.Model(mesh, ctx=ctx)
+    m.set_eqload(0.05, 0.0, 0.0)
+    _, _, ext = m.stiffness(want_k=False)
+    assert rel(ext, ext_o) <= 1e-12
+    # the same factors through the deck reader
+    deck = meshgen.write_deck(mesh, str(tmp_path))
+    with open(deck, "a") as f:
+        f.write("eqload: eqkx=0.05, eqky=0.0, eqkz=0.0\n")
+    md = sg.Model(None, deck=deck, ctx=ctx)
+    _, _, ext_d = md.stiffness(want_k=False)
+    assert np.array_equal(ext_d, ext)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=2000)
+    (r,), x = m.trials([1.0], ctl, want_x=True)
+    ro = om.trial(1.0, want_x=True)
+    assert r["nl_iter"] == ro["nl_iter"] and r["failed"] == ro["failed"]
+    assert rel(x[0], ro["x"]) <= TRIAL_TOL

@@ -229,3 +229,28 @@ def test_trial_rounding_noise_floor():
                 assert max(spread) > 5e-6     # the yield-flip mode is reached by some orders
     finally:
         L.orc_set_dot_order(0)
+
+def _node_dofs(om):
+    """(x, y, z) dof numbers of every element node with all three dofs free."""
+    ge = np.asarray(om.arrays()["gdof_elmt"]).reshape(om.nelmt, 27, 3)
+    rows = {tuple(r) for r in ge.reshape(-1, 3).tolist() if min(r) > 0}
+    return np.array(sorted(rows))
+
+
+def test_pseudo_static_load_known_answer():
+    """The pseudo-static load of src/preprocess.f90:137-143 puts eqk * gamma *
+    w detJ on each node and direction, beside the gravity load -gamma * w detJ
+    on the z dof: on every fully free node the x, y and z loads are -eqkx,
+    -eqky and (1 - eqkz) times the gravity-only z load."""
+    mesh = meshgen.slope2d()
+    _, _, g0 = OracleModel(mesh).stiffness_bodyload()
+    om = OracleModel(mesh)
+    om.set_eqload(0.1, 0.05, 0.02)
+    _, _, g1 = om.stiffness_bodyload()
+    dofs = _node_dofs(om)
+    gz = g0[dofs[:, 2]]
+    assert np.all(gz < 0)
+    np.testing.assert_allclose(g1[dofs[:, 0]], -0.1 * gz, rtol=1e-12)
+    np.testing.assert_allclose(g1[dofs[:, 1]], -0.05 * gz, rtol=1e-12)
+    np.testing.assert_allclose(g1[dofs[:, 2]], 0.98 * gz, rtol=1e-12)
+    assert np.all(g0[dofs[:, 0]] == 0) and np.all(g0[dofs[:, 1]] == 0)
