@@ -175,6 +175,25 @@ int sg_batch_end(sg_model* model);
 
 /* Stress state of the last trial batch: stress[(t*nelmt + e)*27*6 + i*6 + s] for trial t. */
 int sg_last_stress(sg_model* model, int trial, double* stress_elmt);
+/* Valency-averaged nodal stress of trial t of the last batch, stress_global[n*6 + s]
+ * (src/slope.F90:419-437: element stresses summed per node in element order, divided
+ * by the node's valency), reduced on the device. */
+int sg_nodal_stress(sg_model* model, int trial, double* stress_global);
+
+/* ---- outputs (host only; no device needed) ----------------------------- */
+/* Summary file (src/semgeotech.F90:315-319, src/slope.F90:213-220): banner, control
+ * values and the column header; then one row per SRF trial (src/slope.F90:409-416):
+ * srf cg_tot nl_iter uxmax umax fmax. */
+int sg_write_summary_header(const char* path, const sg_control* ctl, int nsrf);
+int sg_write_summary_row(const char* path, const sg_trial_result* result);
+/* EnSight Gold C-binary output (src/semgeotech.F90:126-312, src/visual.f90):
+ * the .case file of a slope run (displacement vector and symmetric stress tensor per
+ * node, one time value per SRF step, files <head>_step<NNN>.dis/.sig), the geometry
+ * (every 27-node element as 8 hexa8 cells, Exodus corner order; g_num 0-based) and one
+ * per-node variable (ncomp 1, 3 or 6; var[n*ncomp + c]). */
+int sg_write_ensight_case(const char* path, const char* head, int nsteps, const double* times, int tstart);
+int sg_write_ensight_geo(const char* path, int nnode, const double* g_coord, int nelmt, const int* g_num);
+int sg_write_ensight_var(const char* path, const char* description, int ncomp, int nnode, const double* var);
 
 /* The slope3d SRF sweep: trials srf[0..nsrf) in order, stopping after the first
  * failed trial (src/slope.F90:441).  Returns the number of trials run in *ndone. */

@@ -46,6 +46,7 @@ def lib():
         L.orc_set_control.argtypes = [vp, d, i, d, i, i, i]
         L.orc_stiffness_bodyload.argtypes = [vp, _dp, _dp, _dp]
         L.orc_set_eqload.argtypes = [vp, d, d, d]
+        L.orc_nodal_stress.argtypes = [vp, _dp, _dp]
         L.orc_pcg_solver.restype = i
         L.orc_pcg_solver.argtypes = [i, i, _dp, _dp, _dp, _dp, _ip, i, d, C.POINTER(C.c_int)]
         L.orc_ebe_apply.argtypes = [i, i, _dp, _dp, _ip, _dp]
@@ -106,6 +107,13 @@ class OracleModel:
         if getattr(self, "h", None):
             lib().orc_free(self.h)
             self.h = None
+
+    def nodal_stress(self, stress_elmt):
+        """Valency-averaged nodal stress [nnode][6] (src/slope.F90:419-437)."""
+        st = np.ascontiguousarray(stress_elmt, np.float64).reshape(-1)
+        out = np.zeros(6 * self.nnode)
+        lib().orc_nodal_stress(self.h, st, out)
+        return out.reshape(-1, 6)
 
     def set_eqload(self, eqkx, eqky, eqkz):
         """Pseudo-static earthquake load factors (src/preprocess.f90:137-143)."""

@@ -1103,6 +1103,23 @@ void* orc_model_from_deck(const char* path) {
 }
 
 void orc_free(void* h) { delete (OrcModel*)h; }
+
+// Valency-averaged nodal stress (src/slope.F90:419-437): stress_global(:,num) +=
+// stress_elmt(:,:,e) over the elements in order, then divided by node_valency.
+void orc_nodal_stress(void* hv, const double* stress_elmt, double* stress_global) {
+  const Model& M = ((OrcModel*)hv)->M;
+  std::vector<int> valency(M.nnode, 0);
+  for (int n = 0; n < M.nnode * NST; ++n) stress_global[n] = 0.0;
+  for (int e = 0; e < M.nelmt; ++e)
+    for (int a = 0; a < NGLL; ++a) {
+      const int n = M.g_num[(size_t)e * NGLL + a];
+      valency[n]++;
+      for (int c = 0; c < NST; ++c)
+        stress_global[(size_t)n * NST + c] = stress_global[(size_t)n * NST + c] + stress_elmt[((size_t)e * NGLL + a) * NST + c];
+    }
+  for (int n = 0; n < M.nnode; ++n)
+    for (int c = 0; c < NST; ++c) stress_global[(size_t)n * NST + c] = stress_global[(size_t)n * NST + c] / (double)valency[n];
+}
 void orc_set_dot_order(int order) { g_dot_order = order; }
 
 void orc_model_sizes(void* hv, int* out /* nnode nelmt neq nmatblk nsrf */) {

@@ -17,6 +17,7 @@ is present the calls raise.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 from typing import Optional, Sequence
 
@@ -34,7 +35,9 @@ PREC_FP64, PREC_MIXED = 0, 1
 EXPORTED = (
     "sg_create", "sg_create_status", "sg_destroy", "sg_last_error", "sg_hbm_used", "sg_pcg_solve",
     "sg_model_from_hex8", "sg_model_from_deck", "sg_model_free", "sg_model_info", "sg_model_arrays",
-    "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
+    "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_nodal_stress",
+    "sg_write_summary_header", "sg_write_summary_row", "sg_write_ensight_case", "sg_write_ensight_geo",
+    "sg_write_ensight_var", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
     "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc",
     "sg_server_create", "sg_server_submit", "sg_server_wait", "sg_server_stats", "sg_server_destroy",
@@ -118,6 +121,18 @@ def lib(path: Optional[str] = None):
     L.sg_model_stiffness.argtypes = [vp, vp, vp, vp]
     L.sg_srf_trials.restype = i
     L.sg_srf_trials.argtypes = [vp, C.POINTER(Control), i, vp, vp, vp]
+    L.sg_nodal_stress.restype = i
+    L.sg_nodal_stress.argtypes = [vp, i, vp]
+    L.sg_write_summary_header.restype = i
+    L.sg_write_summary_header.argtypes = [C.c_char_p, C.POINTER(Control), i]
+    L.sg_write_summary_row.restype = i
+    L.sg_write_summary_row.argtypes = [C.c_char_p, C.POINTER(TrialResult)]
+    L.sg_write_ensight_case.restype = i
+    L.sg_write_ensight_case.argtypes = [C.c_char_p, C.c_char_p, i, vp, i]
+    L.sg_write_ensight_geo.restype = i
+    L.sg_write_ensight_geo.argtypes = [C.c_char_p, i, vp, i, vp]
+    L.sg_write_ensight_var.restype = i
+    L.sg_write_ensight_var.argtypes = [C.c_char_p, C.c_char_p, i, i, vp]
     L.sg_model_set_eqload.restype = i
     L.sg_model_set_eqload.argtypes = [vp, d, d, d]
     L.sg_last_stress.restype = i
@@ -340,6 +355,19 @@ class Model:
             raise SgError(st, self.ctx.last_error)
         return (km.reshape(self.nelmt, 81, 81) if want_k else None), dp, ext
 
+    def nodal_stress(self, trial: int = 0):
+        """Valency-averaged nodal stress [nnode][6] of a trial of the last batch."""
+        out = np.zeros(6 * self.nnode)
+        st = lib().sg_nodal_stress(self.h, trial, _ptr(out))
+        if st:
+            raise SgError(st, "sg_nodal_stress")
+        return out.reshape(-1, 6)
+
+    def nodal_displacement(self, x: np.ndarray):
+        """nodalu[nnode][3] from a solution x(0:neq) (src/slope.F90:400-407)."""
+        gdof = self.arrays()["gdof"]
+        return np.where(gdof > 0, np.asarray(x)[gdof], 0.0)
+
     def set_eqload(self, eqkx: float, eqky: float, eqkz: float):
         """Pseudo-static earthquake load factors (the deck's eqload: line)."""
         st = lib().sg_model_set_eqload(self.h, eqkx, eqky, eqkz)
@@ -478,3 +506,48 @@ class Server:
             self.h = None
 
     __del__ = close
+
+
+def write_summary(path: str, ctl: Control, results, nsrf: Optional[int] = None):
+    """Summary file of a slope run (header, then one row per trial result dict)."""
+    st = lib().sg_write_summary_header(path.encode(), C.byref(ctl), len(results) if nsrf is None else nsrf)
+    if st:
+        raise SgError(st, "sg_write_summary_header")
+    for r in results:
+        tr = TrialResult()
+        for name, _ in TrialResult._fields_:
+            if name in r:
+                setattr(tr, name, r[name])
+        st = lib().sg_write_summary_row(path.encode(), C.byref(tr))
+        if st:
+            raise SgError(st, "sg_write_summary_row")
+
+
+def write_ensight(out_dir: str, head: str, g_coord: np.ndarray, g_num: np.ndarray, times, steps):
+    """EnSight Gold output of a slope run: <head>.case, <head>.geo and, for each
+    step (nodalu[nnode][3], stress_global[nnode][6] or None), <head>_stepNN.dis/.sig."""
+    os.makedirs(out_dir, exist_ok=True)
+    times = np.ascontiguousarray(times, np.float64)
+    nt = len(times)
+    tw = int(math.ceil(math.log10(nt + 1.0)))
+    L = lib()
+
+    def chk(st, what):
+        if st:
+            raise SgError(st, what)
+
+    chk(L.sg_write_ensight_case(os.path.join(out_dir, head + ".case").encode(), head.encode(), nt, _ptr(times), 1),
+        "sg_write_ensight_case")
+    gc = np.ascontiguousarray(g_coord, np.float64).reshape(-1)
+    gn = np.ascontiguousarray(g_num, np.int32).reshape(-1)
+    chk(L.sg_write_ensight_geo(os.path.join(out_dir, head + ".geo").encode(), gc.size // 3, _ptr(gc), gn.size // 27,
+                               _ptr(gn)), "sg_write_ensight_geo")
+    for i, (u, sig) in enumerate(steps):
+        stem = os.path.join(out_dir, f"{head}_step{i + 1:0{tw}d}")
+        u = np.ascontiguousarray(u, np.float64).reshape(-1)
+        chk(L.sg_write_ensight_var((stem + ".dis").encode(), b"Displacement field", 3, u.size // 3, _ptr(u)),
+            "sg_write_ensight_var")
+        if sig is not None:
+            sg_ = np.ascontiguousarray(sig, np.float64).reshape(-1)
+            chk(L.sg_write_ensight_var((stem + ".sig").encode(), b"Effective stress tensor", 6, sg_.size // 6,
+                                       _ptr(sg_)), "sg_write_ensight_var")

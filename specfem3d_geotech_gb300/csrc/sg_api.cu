@@ -1267,6 +1267,36 @@ int sg_last_stress(sg_model* M, int trial, double* stress_elmt) {
   return SG_OK;
 }
 
+int sg_nodal_stress(sg_model* M, int trial, double* stress_global) {
+  if (!M || !stress_global || trial < 0 || trial >= M->W.KR || !M->W.stress) return SG_ERR_BADARG;
+  sg_ctx* c = M->ctx;
+  const HostMesh& h = M->H;
+  // node -> element slots (e*27+a) in increasing element order: the order in
+  // which src/slope.F90:427-431 adds the element stresses
+  std::vector<int> ptr(h.nnode + 1, 0), slot((size_t)h.nelmt * NGLL);
+  for (int t = 0; t < h.nelmt * NGLL; ++t) ptr[h.g_num[t] + 1]++;
+  for (int n = 0; n < h.nnode; ++n) ptr[n + 1] += ptr[n];
+  std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+  for (int t = 0; t < h.nelmt * NGLL; ++t) slot[fill[h.g_num[t]]++] = t;
+  int* d_ptr = c->alloc<int>(ptr.size());
+  int* d_slot = c->alloc<int>(slot.size());
+  double* d_out = c->alloc<double>((size_t)h.nnode * NST);
+  int st = SG_OK;
+  if (!d_ptr || !d_slot || !d_out) {
+    st = SG_ERR_OOM;
+  } else {
+    cudaStream_t s = c->stream;
+    cudaMemcpyAsync(d_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_slot, slot.data(), sizeof(int) * slot.size(), cudaMemcpyHostToDevice, s);
+    const double* stress = M->W.stress + (size_t)trial * h.nelmt * NGLL * NST;
+    launch_nodal_average(d_ptr, d_slot, h.nnode, stress, d_out, s);
+    cudaMemcpyAsync(stress_global, d_out, sizeof(double) * h.nnode * NST, cudaMemcpyDeviceToHost, s);
+    if (!c->check(cudaStreamSynchronize(s), "nodal stress")) st = SG_ERR_CUDA;
+  }
+  for (void* p : {(void*)d_ptr, (void*)d_slot, (void*)d_out}) c->release(p);
+  return st;
+}
+
 int sg_srf_sweep(sg_model* M, const sg_control* ctl, int nsrf, const double* srf, sg_trial_result* results,
                  int* ndone) {
   if (!M || nsrf < 1) return SG_ERR_BADARG;

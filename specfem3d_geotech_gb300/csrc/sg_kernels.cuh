@@ -64,6 +64,8 @@ void launch_apply_mf(const float* rec, const int* ge, int nelmt, const float* po
 void launch_mf_record(const double* geo, const int* mat_id, const int* elist, int nel, const double* ym,
                       const double* nu, float* rec, cudaStream_t s);
 constexpr int MF_REC = 12;        // floats per GLL point of the matrix-free record
+void launch_nodal_average(const int* ptr, const int* slot, int nnode, const double* stress, double* out,
+                          cudaStream_t s);  // sg_output.cu
 bool fp32_matrix_free(int nelmt);  // the FP32 operator of the mixed solve is applied matrix-free
 void set_gather_variant(int v);  // 1 row-cooperative gather for FP32 with 4/8/16 RHS (default), 0 staged
 template <typename V, int KR>

@@ -433,3 +433,20 @@ def test_pseudo_static_load_matches_oracle(ctx, tmp_path):
     ro = om.trial(1.0, want_x=True)
     assert r["nl_iter"] == ro["nl_iter"] and r["failed"] == ro["failed"]
     assert rel(x[0], ro["x"]) <= TRIAL_TOL
+
+
+def test_nodal_stress_matches_oracle(ctx, slope):
+    """The device's valency-averaged nodal stress (src/slope.F90:419-437) is
+    bitwise the oracle's average of the same element stresses, and within the
+    stress tolerance of the oracle's own trial."""
+    mesh, om = slope
+    m = sg.Model(mesh, ctx=ctx)
+    (r,), x = m.trials([1.0], sg.make_control(), want_x=True)
+    st = m.last_stress(0)
+    ns = m.nodal_stress(0)
+    assert np.array_equal(ns, om.nodal_stress(st))
+    ro = om.trial(1.0, want_x=True, want_stress=True)
+    ns_o = om.nodal_stress(ro["stress"])
+    assert np.abs(ns - ns_o).max() <= STRESS_TOL * np.abs(ns_o).max()
+    u = m.nodal_displacement(x[0])
+    assert u.shape == (m.nnode, 3) and abs(np.abs(u).max() - r["uxmax"]) <= 1e-12 * r["uxmax"]
