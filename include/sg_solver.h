@@ -181,6 +181,10 @@ int sg_last_stress(sg_model* model, int trial, double* stress_elmt);
 int sg_nodal_stress(sg_model* model, int trial, double* stress_global);
 
 /* ---- outputs (host only; no device needed) ----------------------------- */
+/* Per node (src/postprocess.f90:146-183): principal stresses psigma[3n..3n+2] in
+ * ascending order (compression first), maximum shear stress taumax[n] = |p1 - p3|/2 and
+ * normal stress on its plane nsigma[n] = (p1 + p3)/2 (taumax, nsigma may be NULL). */
+int sg_principal_stress(int nnode, const double* stress_global, double* psigma, double* taumax, double* nsigma);
 /* Summary file (src/semgeotech.F90:315-319, src/slope.F90:213-220): banner, control
  * values and the column header; then one row per SRF trial (src/slope.F90:409-416):
  * srf cg_tot nl_iter uxmax umax fmax. */

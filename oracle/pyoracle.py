@@ -47,6 +47,7 @@ def lib():
         L.orc_stiffness_bodyload.argtypes = [vp, _dp, _dp, _dp]
         L.orc_set_eqload.argtypes = [vp, d, d, d]
         L.orc_nodal_stress.argtypes = [vp, _dp, _dp]
+        L.orc_principal_stress.argtypes = [i, _dp, _dp, _dp, _dp]
         L.orc_pcg_solver.restype = i
         L.orc_pcg_solver.argtypes = [i, i, _dp, _dp, _dp, _dp, _ip, i, d, C.POINTER(C.c_int)]
         L.orc_ebe_apply.argtypes = [i, i, _dp, _dp, _ip, _dp]
@@ -194,3 +195,12 @@ def pcg_solver(neq, nelmt, k, u, f, dprecon, gdof_elmt, cg_maxiter, cg_tol):
                                np.ascontiguousarray(gdof_elmt, np.int32).reshape(-1), cg_maxiter, cg_tol,
                                C.byref(it))
     return err, it.value
+
+
+def principal_stress(stress_global):
+    """Oracle of src/postprocess.f90:146-183: (psigma[n][3], taumax[n], nsigma[n])."""
+    st = np.ascontiguousarray(stress_global, np.float64).reshape(-1)
+    n = st.size // 6
+    ps, tm, ns = np.zeros(3 * n), np.zeros(n), np.zeros(n)
+    lib().orc_principal_stress(n, st, ps, tm, ns)
+    return ps.reshape(n, 3), tm, ns

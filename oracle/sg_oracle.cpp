@@ -1257,6 +1257,29 @@ void orc_tables(double* gll_w /*27*/, double* dlag /*3*27*27*/, double* dshape /
 }
 void orc_cmat(double E, double nu, double* c) { compute_cmat(E, nu, (double(*)[6])c); }
 void orc_stress_invariant(const double* s, double* out) { stress_invariant(s, out[0], out[1], out[2]); }
+
+// Principal stresses, maximum shear and normal stress per node
+// (src/postprocess.f90:146-183; rquick_sort src/math_library.f90:211-228).
+void orc_principal_stress(int nnode, const double* stress_global, double* psigma, double* taumax, double* nsigma) {
+  const double pi = 3.141592653589793, two_third = 2.0 / 3.0;
+  for (int n = 0; n < nnode; ++n) {
+    double sigm, dsbar, theta;
+    stress_invariant(stress_global + (size_t)6 * n, sigm, dsbar, theta);
+    double x[3];
+    x[0] = sigm + two_third * dsbar * std::sin(theta - two_third * pi);
+    x[1] = sigm + two_third * dsbar * std::sin(theta);
+    x[2] = sigm + two_third * dsbar * std::sin(theta + two_third * pi);
+    for (int i = 1; i < 3; ++i) {
+      double temp = x[i];
+      int j = i - 1;
+      while (j >= 0 && x[j] > temp) { x[j + 1] = x[j]; j = j - 1; }
+      x[j + 1] = temp;
+    }
+    for (int c = 0; c < 3; ++c) psigma[3 * n + c] = x[c];
+    taumax[n] = 0.5 * std::fabs(x[0] - x[2]);
+    nsigma[n] = 0.5 * (x[0] + x[2]);
+  }
+}
 double orc_mohcouf(double phi, double c, double sigm, double dsbar, double theta) {
   return mohcouf(phi, c, sigm, dsbar, theta);
 }

@@ -36,7 +36,7 @@ EXPORTED = (
     "sg_create", "sg_create_status", "sg_destroy", "sg_last_error", "sg_hbm_used", "sg_pcg_solve",
     "sg_model_from_hex8", "sg_model_from_deck", "sg_model_free", "sg_model_info", "sg_model_arrays",
     "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_nodal_stress",
-    "sg_write_summary_header", "sg_write_summary_row", "sg_write_ensight_case", "sg_write_ensight_geo",
+    "sg_principal_stress", "sg_write_summary_header", "sg_write_summary_row", "sg_write_ensight_case", "sg_write_ensight_geo",
     "sg_write_ensight_var", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
     "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc",
@@ -123,6 +123,8 @@ def lib(path: Optional[str] = None):
     L.sg_srf_trials.argtypes = [vp, C.POINTER(Control), i, vp, vp, vp]
     L.sg_nodal_stress.restype = i
     L.sg_nodal_stress.argtypes = [vp, i, vp]
+    L.sg_principal_stress.restype = i
+    L.sg_principal_stress.argtypes = [i, vp, vp, vp, vp]
     L.sg_write_summary_header.restype = i
     L.sg_write_summary_header.argtypes = [C.c_char_p, C.POINTER(Control), i]
     L.sg_write_summary_row.restype = i
@@ -551,3 +553,14 @@ def write_ensight(out_dir: str, head: str, g_coord: np.ndarray, g_num: np.ndarra
             sg_ = np.ascontiguousarray(sig, np.float64).reshape(-1)
             chk(L.sg_write_ensight_var((stem + ".sig").encode(), b"Effective stress tensor", 6, sg_.size // 6,
                                        _ptr(sg_)), "sg_write_ensight_var")
+
+
+def principal_stress(stress_global: np.ndarray):
+    """(psigma[n][3] ascending, taumax[n], nsigma[n]) from nodal stresses [n][6]."""
+    st = np.ascontiguousarray(stress_global, np.float64).reshape(-1)
+    n = st.size // 6
+    ps, tm, ns = np.zeros(3 * n), np.zeros(n), np.zeros(n)
+    r = lib().sg_principal_stress(n, _ptr(st), _ptr(ps), _ptr(tm), _ptr(ns))
+    if r:
+        raise SgError(r, "sg_principal_stress")
+    return ps.reshape(n, 3), tm, ns

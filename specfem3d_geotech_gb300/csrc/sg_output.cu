@@ -9,6 +9,8 @@
 //   "SRF, CGITER, NLITER, UXMAX, UMAX, fmax".  The reference writes these
 //   with Fortran list-directed output; the same lines and fields are written
 //   here as blank-separated values with full precision.
+// * Principal stresses, maximum shear stress and the normal stress on its
+//   plane per node (src/postprocess.f90:146-183).
 // * EnSight Gold C-binary files (src/visual.f90:75-290,
 //   src/semgeotech.F90:126-312, src/postprocess.f90:128-248): the .case
 //   file, the geometry with every 27-node element written as its 8 hexa8
@@ -79,9 +81,54 @@ std::string fortran_e12_5(double v) {
   return pad;
 }
 
+// stress invariants of a 6-component stress (src/math_library.f90:144-186):
+// mean stress, sqrt(3 J2) with J2 clamped at 1e-12, Lode angle
+void invariants(const double* st, double& sigm, double& dsbar, double& theta) {
+  const double sq3 = std::sqrt(3.0), small = 1e-12;
+  const double s1 = st[0], s2 = st[1], s3 = st[2], s4 = st[3], s5 = st[4], s6 = st[5];
+  sigm = (s1 + s2 + s3) / 3.0;
+  double d2 = ((s1 - s2) * (s1 - s2) + (s2 - s3) * (s2 - s3) + (s3 - s1) * (s3 - s1)) / 6.0 + s4 * s4 + s5 * s5 +
+              s6 * s6;
+  if (d2 < small) d2 = small;
+  const double ds1 = s1 - sigm, ds2 = s2 - sigm, ds3 = s3 - sigm;
+  const double d3 = ds1 * ds2 * ds3 - ds1 * s5 * s5 - ds2 * s6 * s6 - ds3 * s4 * s4 + 2.0 * s4 * s5 * s6;
+  dsbar = sq3 * std::sqrt(d2);
+  if (dsbar < small) {
+    theta = 0.0;
+  } else {
+    const double r = std::sqrt(d2);
+    double sine = -3.0 * sq3 * d3 / (2.0 * (r * r * r));
+    if (sine >= 1.0) sine = 1.0;
+    if (sine < -1.0) sine = -1.0;
+    theta = std::asin(sine) / 3.0;
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+int sg_principal_stress(int nnode, const double* stress_global, double* psigma, double* taumax, double* nsigma) {
+  if (nnode < 0 || !stress_global || !psigma) return SG_ERR_BADARG;
+  const double pi = 3.141592653589793, two_third = 2.0 / 3.0;
+  for (int n = 0; n < nnode; ++n) {
+    double sigm, dsbar, theta;
+    invariants(stress_global + (size_t)6 * n, sigm, dsbar, theta);
+    double p[3] = {sigm + two_third * dsbar * std::sin(theta - two_third * pi), sigm + two_third * dsbar * std::sin(theta),
+                   sigm + two_third * dsbar * std::sin(theta + two_third * pi)};
+    // ascending (compression negative first), insertion sort as rquick_sort
+    for (int i = 1; i < 3; ++i) {
+      const double t = p[i];
+      int j = i - 1;
+      while (j >= 0 && p[j] > t) { p[j + 1] = p[j]; --j; }
+      p[j + 1] = t;
+    }
+    for (int c = 0; c < 3; ++c) psigma[(size_t)3 * n + c] = p[c];
+    if (taumax) taumax[n] = 0.5 * std::fabs(p[0] - p[2]);
+    if (nsigma) nsigma[n] = 0.5 * (p[0] + p[2]);
+  }
+  return SG_OK;
+}
 
 int sg_write_summary_header(const char* path, const sg_control* ctl, int nsrf) {
   if (!path || !ctl || nsrf < 0) return SG_ERR_BADARG;

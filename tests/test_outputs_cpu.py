@@ -101,3 +101,26 @@ def test_summary_file(tmp_path):
         f = l.split()
         assert float(f[0]) == r["srf"] and int(f[1]) == r["cg_tot"] and int(f[2]) == r["nl_iter"]
         assert [float(v) for v in f[3:]] == [r["uxmax"], r["umax"], r["fmax"]]
+
+
+def test_principal_stress_matches_oracle():
+    """Principal stresses (ascending), maximum shear and normal stress per node
+    (src/postprocess.f90:146-183) against the oracle, including hydrostatic
+    states (J2 clamp) and the Lode corners; and the exact eigenvalues of the
+    stress tensor."""
+    from oracle import pyoracle
+    rng = np.random.default_rng(1)
+    st = rng.standard_normal((500, 6)) * 50.0
+    st[0] = [-10, -10, -10, 0, 0, 0]          # hydrostatic
+    st[1] = [-30, -10, -10, 0, 0, 0]          # Lode corner
+    st[2] = [-10, -30, -30, 0, 0, 0]
+    ps, tm, ns = sg.principal_stress(st)
+    po, to, no = pyoracle.principal_stress(st)
+    np.testing.assert_allclose(ps, po, rtol=1e-12, atol=1e-9)
+    np.testing.assert_allclose(tm, to, rtol=1e-12, atol=1e-9)
+    np.testing.assert_allclose(ns, no, rtol=1e-12, atol=1e-9)
+    assert np.all(np.diff(ps, axis=1) >= 0)
+    for k in range(3, 50):
+        s = st[k]
+        T = np.array([[s[0], s[3], s[5]], [s[3], s[1], s[4]], [s[5], s[4], s[2]]])
+        np.testing.assert_allclose(ps[k], np.linalg.eigvalsh(T), rtol=1e-9, atol=1e-9)
