@@ -247,6 +247,12 @@ void sg_server_destroy(sg_server* server);
 int sg_excavation(sg_model* model, const sg_control* ctl, int s0_type, double z0, double s0,
                   double k0, int nexcav, const int* nexcavid, const int* excavid, int ninc,
                   double srf, double* stage_res, int* nstage);
+/* Nodal fields of the last completed excavation stage (src/excavation.F90:597-661):
+ * vmeps[n], the von Mises effective plastic strain sqrt(2/3 evpt.evpt) summed over the
+ * intact elements at node n and divided by its intact valency, and scf[n], the smallest
+ * safety factor (sigm sin(phi) - c cos(phi)) / (-dsbar (cos(theta)/sqrt(3) -
+ * sin(theta) sin(phi)/3)) of those points (1e32 where none).  Either may be NULL. */
+int sg_excavation_fields(const sg_model* model, double* vmeps, double* scf);
 
 /* ---- timing of the device work of the last call ----------------------- */
 /* ms[0] total, ms[1] element apply, ms[2] gather, ms[3] PCG vector update,

@@ -72,7 +72,7 @@ def lib():
         L.orc_mohcouq.argtypes = [d, d, d, _dp]
         L.orc_formm.argtypes = [_dp, _dp]
         L.orc_excavation.restype = i
-        L.orc_excavation.argtypes = [vp, i, d, d, d, i, _ip, _ip, i, d, _dp, vp]
+        L.orc_excavation.argtypes = [vp, i, d, d, d, i, _ip, _ip, i, d, _dp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -178,12 +178,19 @@ class OracleModel:
         v = lib().orc_fos_bisection(self.h, lo, hi, step, C.byref(nt))
         return v, nt.value
 
-    def excavation(self, s0_type, z0, s0, k0, excavid, ninc=1, srf=1.0, nexcavid=None):
+    def excavation(self, s0_type, z0, s0, k0, excavid, ninc=1, srf=1.0, nexcavid=None, want_fields=False):
+        """Stage results [stage, cg_tot, nl_tot, uxmax, umax, fmax, failed, errcode]; with
+        want_fields also the last stage's nodal vmeps and scf (src/excavation.F90:597-661)."""
         excavid = np.ascontiguousarray(excavid, np.int32)
         nexcav = len(excavid) if nexcavid is None else len(nexcavid)
         nexcavid = np.ones(nexcav, np.int32) if nexcavid is None else np.ascontiguousarray(nexcavid, np.int32)
         res = np.zeros(8 * nexcav)
-        n = lib().orc_excavation(self.h, s0_type, z0, s0, k0, nexcav, nexcavid, excavid, ninc, srf, res, None)
+        vm = np.zeros(self.nnode) if want_fields else None
+        sf = np.zeros(self.nnode) if want_fields else None
+        n = lib().orc_excavation(self.h, s0_type, z0, s0, k0, nexcav, nexcavid, excavid, ninc, srf, res, None,
+                                 None if vm is None else vm.ctypes.data, None if sf is None else sf.ctypes.data)
+        if want_fields:
+            return res.reshape(-1, 8)[:n], vm, sf
         return res.reshape(-1, 8)[:n]
 
 

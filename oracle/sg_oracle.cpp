@@ -1294,7 +1294,8 @@ void orc_formm(const double* s, double* m) {
 // Returns the number of stages run.
 // ---------------------------------------------------------------------------
 int orc_excavation(void* hv, int s0_type, double z0, double s0, double k0, int nexcav, const int* nexcavid,
-                   const int* excavid, int ninc, double srf, double* res, double* x_last) {
+                   const int* excavid, int ninc, double srf, double* res, double* x_last, double* vmeps_out,
+                   double* scf_out) {
   OrcModel* h = (OrcModel*)hv;
   Model M = h->M;  // gdof is renumbered per stage
   const Control& C = h->C;
@@ -1333,6 +1334,8 @@ int orc_excavation(void* hv, int s0_type, double z0, double s0, double k0, int n
     if (nelmt_intact <= 0) break;
     std::vector<char> isnode(M.nnode, 0);
     for (int e : eint) for (int a = 0; a < NGLL; ++a) isnode[M.g_num[(size_t)e * NGLL + a]] = 1;
+    // per-stage fields (src/excavation.F90:335): vmeps = 0, scf = inftol
+    std::vector<double> vmeps(M.nnode, 0.0), scf(M.nnode, INFTOL);
     // modify_gdof (src/excavation_library.f90:90-111)
     for (int j = 0; j < M.nnode; ++j) if (!isnode[j]) for (int d = 0; d < 3; ++d) M.gdof[(size_t)3 * j + d] = 0;
     int neq = 0;
@@ -1413,7 +1416,7 @@ int orc_excavation(void* hv, int s0_type, double z0, double s0, double k0, int n
         bool fin = nl_isconv || nl_iter == C.nl_maxiter;
         fmax = stress_update(M, eint.data(), nelmt_intact, x.data(), M.gdof_elmt.data(), M.ym.data(), nuf.data(),
                              phif.data(), cohf.data(), psif.data(), dt, nl_isconv, fin, evpt.data(), stress.data(),
-                             bodyload.data(), nullptr, nullptr);
+                             bodyload.data(), vmeps.data(), scf.data());
         if (fin) break;
       }
       if (errcode != 0) break;
@@ -1424,6 +1427,15 @@ int orc_excavation(void* hv, int s0_type, double z0, double s0, double k0, int n
           if (g) nodalu[(size_t)3 * j + d] += x[g];
         }
       if (x_last && is == nexcav - 1 && inc == ninc - 1) std::memcpy(x_last, x.data(), sizeof(double) * n1);
+    }
+    // average effective plastic strain over the intact valency (src/excavation.F90:656-661)
+    {
+      std::vector<int> valency(M.nnode, 0);
+      for (int e : eint) for (int a = 0; a < NGLL; ++a) valency[M.g_num[(size_t)e * NGLL + a]]++;
+      for (int j = 0; j < M.nnode; ++j)
+        if (isnode[j]) vmeps[j] = vmeps[j] / (double)valency[j];
+      if (vmeps_out) std::memcpy(vmeps_out, vmeps.data(), sizeof(double) * M.nnode);
+      if (scf_out) std::memcpy(scf_out, scf.data(), sizeof(double) * M.nnode);
     }
     double uxmax = 0, umax = 0;
     for (int j = 0; j < M.nnode; ++j) {

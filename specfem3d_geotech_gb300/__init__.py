@@ -35,7 +35,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 EXPORTED = (
     "sg_create", "sg_create_status", "sg_destroy", "sg_last_error", "sg_hbm_used", "sg_pcg_solve",
     "sg_model_from_hex8", "sg_model_from_deck", "sg_model_free", "sg_model_info", "sg_model_arrays",
-    "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_nodal_stress",
+    "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_nodal_stress", "sg_excavation_fields",
     "sg_principal_stress", "sg_write_summary_header", "sg_write_summary_row", "sg_write_ensight_case", "sg_write_ensight_geo",
     "sg_write_ensight_var", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
@@ -121,6 +121,8 @@ def lib(path: Optional[str] = None):
     L.sg_model_stiffness.argtypes = [vp, vp, vp, vp]
     L.sg_srf_trials.restype = i
     L.sg_srf_trials.argtypes = [vp, C.POINTER(Control), i, vp, vp, vp]
+    L.sg_excavation_fields.restype = i
+    L.sg_excavation_fields.argtypes = [vp, vp, vp]
     L.sg_nodal_stress.restype = i
     L.sg_nodal_stress.argtypes = [vp, i, vp]
     L.sg_principal_stress.restype = i
@@ -356,6 +358,14 @@ class Model:
         if st:
             raise SgError(st, self.ctx.last_error)
         return (km.reshape(self.nelmt, 81, 81) if want_k else None), dp, ext
+
+    def excavation_fields(self):
+        """(vmeps[nnode], scf[nnode]) of the last excavation stage."""
+        vm, sf = np.zeros(self.nnode), np.zeros(self.nnode)
+        st = lib().sg_excavation_fields(self.h, _ptr(vm), _ptr(sf))
+        if st:
+            raise SgError(st, "sg_excavation_fields")
+        return vm, sf
 
     def nodal_stress(self, trial: int = 0):
         """Valency-averaged nodal stress [nnode][6] of a trial of the last batch."""

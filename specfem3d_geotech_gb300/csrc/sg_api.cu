@@ -580,6 +580,7 @@ struct sg_model {
   double* d_Yscratch = nullptr;  // nelmt*81 (diag / gravity element vectors)
   TrialWork W;
   std::vector<double> last_stress_ok;
+  std::vector<double> ex_vmeps, ex_scf;  // nodal fields of the last excavation stage
   double* d_fpart = nullptr;
 };
 
@@ -1267,6 +1268,13 @@ int sg_last_stress(sg_model* M, int trial, double* stress_elmt) {
   return SG_OK;
 }
 
+int sg_excavation_fields(const sg_model* M, double* vmeps, double* scf) {
+  if (!M || M->ex_vmeps.empty()) return SG_ERR_BADARG;
+  if (vmeps) std::memcpy(vmeps, M->ex_vmeps.data(), sizeof(double) * M->ex_vmeps.size());
+  if (scf) std::memcpy(scf, M->ex_scf.data(), sizeof(double) * M->ex_scf.size());
+  return SG_OK;
+}
+
 int sg_nodal_stress(sg_model* M, int trial, double* stress_global) {
   if (!M || !stress_global || trial < 0 || trial >= M->W.KR || !M->W.stress) return SG_ERR_BADARG;
   sg_ctx* c = M->ctx;
@@ -1447,8 +1455,13 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
       int* d_geint = c->alloc<int>(ge_int.size());
       int* d_geall = c->alloc<int>(ge_all.size());
       int* d_gdofn = c->alloc<int>(gdof.size());
-      bool ok = d_eint && d_evoid && d_geint && d_geall && d_gdofn && upload_topo(c, Ti) && upload_topo(c, Tv) &&
-                model_work(M, 1, n1, nint);
+      // per-point effective plastic strain and safety factor of the finalize pass
+      double* d_vm = c->alloc<double>((size_t)nint * NGLL);
+      double* d_sf = c->alloc<double>((size_t)nint * NGLL);
+      // per-stage nodal fields (src/excavation.F90:335): vmeps = 0, scf = inftol
+      std::vector<double> vmeps(h.nnode, 0.0), scf(h.nnode, 1.0e32);
+      bool ok = d_eint && d_evoid && d_geint && d_geall && d_gdofn && d_vm && d_sf && upload_topo(c, Ti) &&
+                upload_topo(c, Tv) && model_work(M, 1, n1, nint);
       if (!ok) {
         status = SG_ERR_OOM;
       } else {
@@ -1498,11 +1511,24 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
             double uerr = red[0] / red[1];
             int conv = uerr <= ctl->nl_tol, fin = conv || nl_iter == ctl->nl_maxiter;
             launch_stress_update(M->d_geo, d_eint, nint, d_geall, M->d_matid, W.x, 1, 0, W.mf, dt, conv, fin, evpt,
-                                 stress, W.Yb, 1, 0, M->d_fpart, Ti.d_pos, s);
+                                 stress, W.Yb, 1, 0, M->d_fpart, Ti.d_pos, s, d_vm, d_sf);
             reduce_read(c, M->d_fpart, NPART, 1, 1, 1, W.red, red);
             fmax = red[0];
             if (!fin) launch_gather_plain<double>(Ti, 1, W.Yb, W.bodyload, 1, nullptr, s);
-            if (fin) break;
+            if (fin) {
+              // vmeps(num(i)) += ..., scf(num(i)) = min(scf, sf) over the intact
+              // elements in order (src/excavation.F90:597-609)
+              std::vector<double> hv((size_t)nint * NGLL), hs((size_t)nint * NGLL);
+              cudaMemcpy(hv.data(), d_vm, sizeof(double) * hv.size(), cudaMemcpyDeviceToHost);
+              cudaMemcpy(hs.data(), d_sf, sizeof(double) * hs.size(), cudaMemcpyDeviceToHost);
+              for (int le = 0; le < nint; ++le)
+                for (int i = 0; i < NGLL; ++i) {
+                  const int nd = h.g_num[(size_t)eint[le] * NGLL + i];
+                  vmeps[nd] = vmeps[nd] + hv[(size_t)le * NGLL + i];
+                  if (hs[(size_t)le * NGLL + i] < scf[nd]) scf[nd] = hs[(size_t)le * NGLL + i];
+                }
+              break;
+            }
           }
           if (nl_iter > ctl->nl_maxiter) nl_iter = ctl->nl_maxiter;
           nl_tot += nl_iter;
@@ -1512,6 +1538,16 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
           for (int j = 0; j < h.nnode; ++j)
             for (int d = 0; d < 3; ++d)
               if (gdof[3 * j + d]) nodalu[3 * j + d] += hx[gdof[3 * j + d]];
+        }
+        // average effective plastic strain over the intact valency (src/excavation.F90:656-661)
+        {
+          std::vector<int> valency(h.nnode, 0);
+          for (int e : eint)
+            for (int a = 0; a < NGLL; ++a) valency[h.g_num[(size_t)e * NGLL + a]]++;
+          for (int j = 0; j < h.nnode; ++j)
+            if (isnode[j]) vmeps[j] = vmeps[j] / (double)valency[j];
+          M->ex_vmeps = vmeps;
+          M->ex_scf = scf;
         }
         double uxmax = 0, umax = 0;
         for (int j = 0; j < h.nnode; ++j) {
@@ -1528,7 +1564,9 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
       }
       free_topo(c, Ti);
       free_topo(c, Tv);
-      for (void* p : {(void*)d_eint, (void*)d_evoid, (void*)d_geint, (void*)d_geall, (void*)d_gdofn}) c->release(p);
+      for (void* p : {(void*)d_eint, (void*)d_evoid, (void*)d_geint, (void*)d_geall, (void*)d_gdofn, (void*)d_vm,
+                      (void*)d_sf})
+        c->release(p);
       if (status != SG_OK || stage_res[8 * is + 6] != 0) break;
     }
     if (nstage) *nstage = stages;

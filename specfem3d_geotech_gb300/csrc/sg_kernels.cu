@@ -1425,7 +1425,8 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
     const double* __restrict__ geo, const int* __restrict__ elist, int nel, const int* __restrict__ ge,
     const int* __restrict__ mat_id, const double* __restrict__ x, int xstride, int xcol, const MatF* __restrict__ mf,
     double dt, int nl_isconv, int finalize, double* __restrict__ evpt, double* __restrict__ stress,
-    double* __restrict__ Yb, int ystride, int ycol, double* __restrict__ fmax_part, const int* __restrict__ pos) {
+    double* __restrict__ Yb, int ystride, int ycol, double* __restrict__ fmax_part, const int* __restrict__ pos,
+    double* __restrict__ vm_pt, double* __restrict__ sf_pt) {
   __shared__ double s_eld[STRESS_WARPS][NEDOF];
   __shared__ double s_q[STRESS_WARPS][NGLL][9];
   __shared__ double s_fmax[STRESS_WARPS];
@@ -1556,6 +1557,17 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
       if (finalize) {
 #pragma unroll
         for (int s = 0; s < 6; ++s) se[s] = eff[s];
+        // excavation fields (src/excavation.F90:599-609): von Mises effective
+        // plastic strain of the updated evpt and the point's safety factor
+        if (vm_pt) {
+          double q2 = 0.0;
+#pragma unroll
+          for (int s = 0; s < 6; ++s) q2 = q2 + ev[s] * ev[s];
+          vm_pt[(size_t)le * NGLL + i] = sqrt((2.0 / r3) * q2);
+        }
+        if (sf_pt)
+          sf_pt[(size_t)le * NGLL + i] =
+              (sigm * m.snph - m.cohf * m.csph) / (-dsbar * (csth / sq3 - snth * m.snph / r3));
       }
 #pragma unroll
       for (int t = 0; t < 9; ++t) s_q[warp][i][t] = q[t];
@@ -1606,11 +1618,11 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
 void launch_stress_update(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
                           const double* x, int xstride, int xcol, const MatF* mf, double dt, int nl_isconv,
                           int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
-                          double* fmax_part, const int* pos, cudaStream_t s) {
+                          double* fmax_part, const int* pos, cudaStream_t s, double* vm_pt, double* sf_pt) {
   // fixed grid so that fmax_part has NPART entries
   SG_LAUNCH k_stress_update<<<NPART, STRESS_WARPS * 32, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, xstride, xcol, mf, dt,
                                                        nl_isconv, finalize, evpt, stress, Yb, ystride, ycol,
-                                                       fmax_part, pos);
+                                                       fmax_part, pos, vm_pt, sf_pt);
 }
 
 // elastic_stress (src/postprocess.f90:40-79): sigma = C B x per GLL point

@@ -84,7 +84,8 @@ void pcg_update(int n1, V* u, V* r, V* z, const V* p, const V* kp, const V* f, c
 void launch_stress_update(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
                           const double* x, int xstride, int xcol, const MatF* mf, double dt, int nl_isconv,
                           int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
-                          double* fmax_part, const int* pos, cudaStream_t s);
+                          double* fmax_part, const int* pos, cudaStream_t s, double* vm_pt = nullptr,
+                          double* sf_pt = nullptr);
 void launch_elastic_stress(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
                            const double* x, int xstride, int xcol, const MatF* mf, int accumulate, double* stress,
                            cudaStream_t s);

@@ -450,3 +450,23 @@ def test_nodal_stress_matches_oracle(ctx, slope):
     assert np.abs(ns - ns_o).max() <= STRESS_TOL * np.abs(ns_o).max()
     u = m.nodal_displacement(x[0])
     assert u.shape == (m.nnode, 3) and abs(np.abs(u).max() - r["uxmax"]) <= 1e-12 * r["uxmax"]
+
+
+def test_excavation_fields_match_oracle(ctx):
+    """The last stage's nodal fields of the excavation driver
+    (src/excavation.F90:597-661): von Mises effective plastic strain averaged
+    over the intact valency and the smallest point safety factor per node."""
+    mesh = meshgen.excavation(nx=6, ny=6, nz=4, L=12.0, H=8.0, pit=4.0, lifts=2, lift_h=2.0)
+    om = OracleModel(mesh)
+    om.set_control(1e-8, 5000, 1e-4, 200)
+    ro, vm_o, sf_o = om.excavation(1, 8.0, 0.0, 0.5, [2, 3], want_fields=True)
+    m = sg.Model(mesh, ctx=ctx)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=200)
+    r = m.excavation(ctl, 1, 8.0, 0.0, 0.5, [2, 3])
+    vm, sf = m.excavation_fields()
+    assert r.shape == ro.shape
+    outside = sf_o == 1e32                       # nodes of removed elements only
+    assert np.array_equal(sf == 1e32, outside) and outside.sum() > 0
+    np.testing.assert_allclose(sf[~outside], sf_o[~outside], rtol=1e-5)
+    scale = max(np.abs(vm_o).max(), 1e-300)
+    assert np.abs(vm - vm_o).max() <= STRESS_TOL * scale
