@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libsg.so")
 SOURCES = ["sg_kernels.cu", "sg_api.cu", "sg_host_mesh.cu", "sg_noalloc.cu", "sg_serve.cu", "sg_apply_tc.cu",
            "sg_apply_lanes.cu", "sg_apply_mf.cu",
-           "sg_output.cu"]
+           "sg_output.cu", "sg_pcg_persist.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
          "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr", "-diag-suppress", "177"]

@@ -266,10 +266,21 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
       (uintptr_t)C->d_nbr, (uintptr_t)B.Y, (uintptr_t)B.kp, (uintptr_t)B.p, (uintptr_t)B.z, (uintptr_t)B.r,
       (uintptr_t)B.cs, (uintptr_t)B.G, (uintptr_t)B.part, (uintptr_t)u, (uintptr_t)f, (uintptr_t)dp,
       (uintptr_t)n1, (uintptr_t)KR, (uintptr_t)sizeof(V), (uintptr_t)chunk, (uintptr_t)0};
+  // small meshes with the matrix-free FP32 operator: the whole chunk as one
+  // persistent cooperative launch (sg_pcg_persist.cu)
+  bool persist = false;
+  if constexpr (std::is_same<V, float>::value && KR <= 8)
+    persist = op.dense == 2 && op.nelmt < 20000 && !C->prof.on && persist_enabled();
   int nchunks = 0;
   while (true) {
-    cudaGraphExec_t ex = (graphs && nchunks > 0) ? C->chunk_graph(key, eager_chunk) : nullptr;
-    if (ex) {
+    bool done_chunk = false;
+    if constexpr (std::is_same<V, float>::value)
+      if (persist)
+        done_chunk = launch_pcg_persistent<KR>((const float*)op.K, op.ge, op.nelmt, op.T->d_pos, *op.T, n1, u, B.r,
+                                               B.z, B.p, B.kp, B.Y, dp, B.cs, B.G, B.part, chunk, s);
+    cudaGraphExec_t ex = (!done_chunk && graphs && nchunks > 0) ? C->chunk_graph(key, eager_chunk) : nullptr;
+    if (done_chunk) {
+    } else if (ex) {
       cudaGraphLaunch(ex, s);
       add_launches(3LL * chunk);
     } else {
@@ -1176,7 +1187,7 @@ static int batch_iteration(sg_model* M) {
     S.res.failed = (S.res.nl_iter == ctl->nl_maxiter);
     slot_finish(M, t);
   }
-  if (apply_error_flag(s) || apply_tc_error_flag(s) || apply_lanes_error_flag(s)) {
+  if (apply_error_flag(s) || apply_tc_error_flag(s) || apply_lanes_error_flag(s) || persist_error_flag(s)) {
     c->err = "element apply: a bounded wait timed out";
     return SG_ERR_TIMEOUT;
   }

@@ -66,7 +66,15 @@ void launch_mf_record(const double* geo, const int* mat_id, const int* elist, in
 constexpr int MF_REC = 12;        // floats per GLL point of the matrix-free record
 void launch_nodal_average(const int* ptr, const int* slot, int nnode, const double* stress, double* out,
                           cudaStream_t s);  // sg_output.cu
-bool fp32_matrix_free(int nelmt);  // the FP32 operator of the mixed solve is applied matrix-free
+bool fp32_matrix_free(int nelmt);
+// Persistent cooperative FP32 PCG chunk for small meshes (sg_pcg_persist.cu);
+// false when it cannot run (the caller launches the separate kernels).
+template <int KR>
+bool launch_pcg_persistent(const float* rec, const int* ge, int nelmt, const int* pos, const GatherTopo& T, int n1,
+                           float* u, float* r, float* z, float* p, float* kp, float* Y, const float* dp,
+                           ColState* cs, PcgGlobal* G, double* part, int chunk, cudaStream_t s);
+bool persist_enabled();                 // SG_PERSIST=0 turns the persistent chunk off
+int persist_error_flag(cudaStream_t s);  // 1 if a persistent chunk's grid barrier timed out  // the FP32 operator of the mixed solve is applied matrix-free
 void set_gather_variant(int v);  // 1 row-cooperative gather for FP32 with 4/8/16 RHS (default), 0 staged
 template <typename V, int KR>
 // Y receives element slot (e, a)'s three rows (x KR) at the slot's gather

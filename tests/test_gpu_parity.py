@@ -470,3 +470,20 @@ def test_excavation_fields_match_oracle(ctx):
     np.testing.assert_allclose(sf[~outside], sf_o[~outside], rtol=1e-5)
     scale = max(np.abs(vm_o).max(), 1e-300)
     assert np.abs(vm - vm_o).max() <= STRESS_TOL * scale
+
+
+@pytest.mark.parametrize("k", [1, 2, 4, 8])
+def test_persistent_pcg_matches_separate_kernels(tmp_path, k):
+    """On small meshes the FP32 PCG iterations run as one persistent
+    cooperative kernel (grid barriers between apply, gather and update; every
+    block recomputes alpha and beta from the partials in a fixed order).  Its
+    trials equal those of the separate kernels to the mixed tolerance with the
+    same plastic-iteration counts, and two runs are bitwise equal."""
+    srfs = [1.0 + 0.03 * t for t in range(k)]
+    a = _variant_trials(0, srfs, tmp_path / "sep.npz", var="SG_PERSIST")
+    b = _variant_trials(1, srfs, tmp_path / "per.npz", var="SG_PERSIST")
+    c = _variant_trials(1, srfs, tmp_path / "per2.npz", var="SG_PERSIST")
+    assert a["nl"].tolist() == b["nl"].tolist()
+    for t in range(k):
+        assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
+    assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
