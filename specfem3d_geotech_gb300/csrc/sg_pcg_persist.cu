@@ -114,7 +114,7 @@ struct Shape {
 };
 
 template <int KR>
-__global__ void __launch_bounds__(NT) k_pcg_persistent(Args A) {
+__global__ void __launch_bounds__(NT, 4) k_pcg_persistent(Args A) {
   using S = Shape<KR>;
   static_assert(S::EPC >= 1, "KR up to 8");
   __shared__ __align__(16) float sU[S::EPC][S::UF];
@@ -153,20 +153,28 @@ __global__ void __launch_bounds__(NT) k_pcg_persistent(Args A) {
     // ---- phase A: element products of p = z + beta p_old (matrix-free) ----
     {
       const float beta = act ? (float)c_beta[ja] : 0.f;
-      for (int e0 = blockIdx.x * S::EPC; e0 < A.nelmt; e0 += grid * S::EPC) {
-        const int e = e0 + el;
+      const int estride = grid * S::EPC;
+      // software pipeline: the next element's p and z values load while this
+      // element computes (its dof numbers one element further ahead)
+      int e = blockIdx.x * S::EPC + el;
+      int gd[3], gdn[3];
+      float pv[3], zv[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gd[c] = (act && e < A.nelmt) ? __ldg(A.ge + (size_t)e * NEDOF + 3 * a + c) : 0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        pv[c] = ldf(A.p + (size_t)gd[c] * KR + ja);
+        zv[c] = ldf(A.z + (size_t)gd[c] * KR + ja);
+      }
+      for (int e0 = blockIdx.x * S::EPC; e0 < A.nelmt; e0 += estride, e += estride) {
         const bool valid = act && e < A.nelmt;
         if (act) {
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            float u = 0.f;
-            if (valid) {
-              const int gd = __ldg(A.ge + (size_t)e * NEDOF + 3 * a + c);
-              u = fmaf(beta, ldf(A.p + (size_t)gd * KR + ja), ldf(A.z + (size_t)gd * KR + ja));
-            }
-            U[(3 * a + c) * KR + ja] = u;
-          }
+          for (int c = 0; c < 3; ++c) U[(3 * a + c) * KR + ja] = valid ? fmaf(beta, pv[c], zv[c]) : 0.f;
         }
+        const int en = e + estride;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gdn[c] = (act && en < A.nelmt) ? __ldg(A.ge + (size_t)en * NEDOF + 3 * a + c) : 0;
         __syncthreads();
         if (valid) {
           const int ic[3] = {a % 3, (a / 3) % 3, a / 9};
@@ -210,6 +218,11 @@ __global__ void __launch_bounds__(NT) k_pcg_persistent(Args A) {
             for (int rr = 0; rr < 3; ++rr)
               F[((3 * a + c) * 3 + rr) * KR + ja] =
                   fmaf(Ji[rr], T[c][0], fmaf(Ji[3 + rr], T[c][1], Ji[6 + rr] * T[c][2]));
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          pv[c] = ldf(A.p + (size_t)gdn[c] * KR + ja);
+          zv[c] = ldf(A.z + (size_t)gdn[c] * KR + ja);
         }
         __syncthreads();
         if (valid) {
