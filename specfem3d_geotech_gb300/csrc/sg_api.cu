@@ -267,13 +267,11 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
       (uintptr_t)B.cs, (uintptr_t)B.G, (uintptr_t)B.part, (uintptr_t)u, (uintptr_t)f, (uintptr_t)dp,
       (uintptr_t)n1, (uintptr_t)KR, (uintptr_t)sizeof(V), (uintptr_t)chunk, (uintptr_t)0};
   // very small meshes with the matrix-free FP32 operator: the whole chunk as
-  // one persistent cooperative launch (sg_pcg_persist.cu).  Measured per PCG
-  // iteration with 8 trials: 22.6 against 34.2 us at 270 elements, 35.9 against
-  // 39.9 us at 1,125; at 3,000 the barrier over ~600 blocks costs more than the
-  // launches it saves (80 against 54 us), hence the bound.
+  // one persistent cooperative launch (sg_pcg_persist.cu), below the size at
+  // which the grid barrier costs more than the launches it saves
   bool persist = false;
   if constexpr (std::is_same<V, float>::value && KR <= 8)
-    persist = op.dense == 2 && op.nelmt < 1500 && !C->prof.on && persist_enabled();
+    persist = op.dense == 2 && op.nelmt < persist_max_elements() && !C->prof.on && persist_enabled();
   int nchunks = 0;
   while (true) {
     bool done_chunk = false;

@@ -74,6 +74,7 @@ bool launch_pcg_persistent(const float* rec, const int* ge, int nelmt, const int
                            float* u, float* r, float* z, float* p, float* kp, float* Y, const float* dp,
                            ColState* cs, PcgGlobal* G, double* part, int chunk, cudaStream_t s);
 bool persist_enabled();                 // SG_PERSIST=0 turns the persistent chunk off
+int persist_max_elements();             // meshes below this use it
 int persist_error_flag(cudaStream_t s);  // 1 if a persistent chunk's grid barrier timed out  // the FP32 operator of the mixed solve is applied matrix-free
 void set_gather_variant(int v);  // 1 row-cooperative gather for FP32 with 4/8/16 RHS (default), 0 staged
 template <typename V, int KR>
