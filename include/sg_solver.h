@@ -100,8 +100,9 @@ sg_model* sg_model_from_hex8(sg_ctx* ctx, int nnode8, const double* x8, const do
                              const double* z8, int nelmt, const int* conn8, const int* mat_id,
                              int nmatblk, const double* props, const int* bc_counts,
                              const int* bc_pairs, int precision, char* errtag);
-/* Reads a serial .sem deck (preinfo/mesh/bc/material/control/stress0 lines,
- * src/read_input.f90:13-619) and builds the model as above. */
+/* Reads a serial .sem deck (preinfo/mesh/bc/material/control/stress0/eqload/water
+ * lines, src/read_input.f90:13-619) and builds the model as above; a water: line
+ * sets the model's pore pressure as sg_model_set_water does. */
 sg_model* sg_model_from_deck(sg_ctx* ctx, const char* sem_path, int precision, char* errtag);
 void sg_model_free(sg_model* model);
 /* info[0..7] = nnode, nelmt, neq, nmatblk, nsrf (deck), ngroups, 0, 0 */
@@ -122,6 +123,22 @@ int sg_model_stiffness(sg_model* model, double* storekm, double* dprecon, double
  * excavation driver keeps gravity alone (src/excavation.F90:191).  Rebuilds the
  * stiffness and loads; SG_ERR_BADARG while a trial batch is open. */
 int sg_model_set_eqload(sg_model* model, double eqkx, double eqky, double eqkz);
+/* Water table (the deck's water: line and the material list's water IDs,
+ * src/read_input.f90:307-317,602-611; compute_pressure, src/compute_pressure.f90:10-186,
+ * replaced on the device): nodes of elements whose material is one of water_ids
+ * (1-based, nwmat of them) are submerged, and a submerged node under the first
+ * surface of wsfile that covers it gets the pore pressure 9.81 (z_surface - z).
+ * Every later slope trial and excavation stage adds that pressure to the normal
+ * components of the effective stress at the node's GLL points (src/slope.F90:334-341,
+ * src/excavation.F90:566-576).  Errors: the file cannot be read, a water ID out of
+ * range, a meshed surface whose z cannot be determined ("ERROR: free surface cannot
+ * be determined!") -> SG_ERR_BADARG with errtag; SG_ERR_BADARG while a trial batch is open. */
+int sg_model_set_water(sg_model* model, const char* wsfile, const int* water_ids, int nwmat, char* errtag);
+/* Sets the pore pressure directly (nnode values, node order of sg_model_arrays;
+ * 0 on nodes that are not submerged); NULL removes it. */
+int sg_model_set_pore_pressure(sg_model* model, const double* wpressure);
+/* Reads the pore pressure back (nnode values); SG_ERR_BADARG when none is set. */
+int sg_model_pore_pressure(const sg_model* model, double* wpressure);
 
 /* ---- one strength-reduction trial of slope3d (src/slope.F90:244-443) ---- */
 typedef struct sg_control {

@@ -46,6 +46,10 @@ def lib():
         L.orc_set_control.argtypes = [vp, d, i, d, i, i, i]
         L.orc_stiffness_bodyload.argtypes = [vp, _dp, _dp, _dp]
         L.orc_set_eqload.argtypes = [vp, d, d, d]
+        L.orc_set_water.restype = i
+        L.orc_set_water.argtypes = [vp, _ip, i, C.c_char_p, C.c_char_p]
+        L.orc_pore_pressure.restype = i
+        L.orc_pore_pressure.argtypes = [vp, vp, vp]
         L.orc_nodal_stress.argtypes = [vp, _dp, _dp]
         L.orc_principal_stress.argtypes = [i, _dp, _dp, _dp, _dp]
         L.orc_pcg_solver.restype = i
@@ -119,6 +123,25 @@ class OracleModel:
     def set_eqload(self, eqkx, eqky, eqkz):
         """Pseudo-static earthquake load factors (src/preprocess.f90:137-143)."""
         lib().orc_set_eqload(self.h, eqkx, eqky, eqkz)
+
+    def set_water(self, water_ids, wsfile: str):
+        """Water table from a water-surface file and the water material IDs
+        (src/compute_pressure.f90:10-186); raises RuntimeError with the
+        reference's message when the pressure cannot be computed."""
+        ids = np.ascontiguousarray(np.asarray(water_ids, np.int32).reshape(-1))
+        tag = C.create_string_buffer(251)
+        st = lib().orc_set_water(self.h, ids if ids.size else np.zeros(1, np.int32), int(ids.size),
+                                 str(wsfile).encode(), tag)
+        if st != 0:
+            raise RuntimeError(tag.value.decode().strip())
+
+    def pore_pressure(self):
+        """(wpressure[nnode], submerged[nnode]) of the water table, or None."""
+        wp = np.zeros(self.nnode)
+        sub = np.zeros(self.nnode, np.int32)
+        if lib().orc_pore_pressure(self.h, wp.ctypes.data, sub.ctypes.data) != 0:
+            return None
+        return wp, sub.astype(bool)
 
     def set_control(self, cg_tol, cg_maxiter, nl_tol, nl_maxiter, phinu=0, allelastic=0):
         lib().orc_set_control(self.h, cg_tol, cg_maxiter, nl_tol, nl_maxiter, phinu, allelastic)

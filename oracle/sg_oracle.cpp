@@ -361,6 +361,9 @@ struct Model {
   std::vector<double> gam, ym, nu, phi, coh, psi;
   std::vector<int> gdof;         // 3*nnode
   std::vector<int> gdof_elmt;    // 81*nelmt
+  bool iswater = false;          // water table set (water: line)
+  std::vector<double> wpressure; // nnode pore pressure
+  std::vector<char> submerged;   // nnode
 };
 
 // get_global (src/mesh_spec.f90:146-262): lexicographic segmented sort with
@@ -472,6 +475,105 @@ void apply_bc(Model& M, const std::vector<std::pair<int, int>> bc[3]) {
     for (int i = 0; i < 3; ++i)
       if (M.gdof[(size_t)3 * j + i] != 0) M.gdof[(size_t)3 * j + i] = ++neq;
   M.neq = neq;
+}
+
+// compute_pressure (src/compute_pressure.f90:10-186).  water[m] flags the water
+// materials; the water-surface file is read list-directed.  Returns 0, or -1
+// with errtag set.
+struct WaterSurf {
+  int stype = 0, rdir = 1;
+  double rx1 = 0, rx2 = 0, z1 = 0, z2 = 0;
+  std::vector<int> ielmt, iface;  // 1-based element, face 1..6
+};
+
+int compute_pressure(Model& M, const std::vector<char>& water, const std::string& wsfile, std::string& errtag) {
+  const Tables& T = tables();
+  const double gamw = 9.81;
+  errtag = "ERROR: unknown!";
+  M.submerged.assign(M.nnode, 0);
+  for (int e = 0; e < M.nelmt; ++e)
+    if (water[M.mat_id[e] - 1])
+      for (int i = 0; i < NGLL; ++i) M.submerged[M.g_num[(size_t)e * NGLL + i]] = 1;
+  std::ifstream in(wsfile);
+  if (!in) { errtag = "ERROR: input file \"" + wsfile + "\" cannot be opened!"; return -1; }
+  std::string all((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+  for (char& ch : all) if (ch == ',') ch = ' ';
+  std::stringstream ss(all);
+  int nwsurf = 0;
+  ss >> nwsurf;
+  std::vector<WaterSurf> ws(nwsurf);
+  for (auto& w : ws) {
+    ss >> w.stype;
+    if (w.stype == 0) ss >> w.rdir >> w.rx1 >> w.rx2 >> w.z1;
+    else if (w.stype == 1) ss >> w.rdir >> w.rx1 >> w.rx2 >> w.z1 >> w.z2;
+    else if (w.stype == 2) {
+      int nface = 0;
+      ss >> nface;
+      w.ielmt.resize(nface); w.iface.resize(nface);
+      for (int f = 0; f < nface; ++f) ss >> w.ielmt[f] >> w.iface[f];
+    }
+  }
+  M.wpressure.assign(M.nnode, 0.0);
+  for (int n = 0; n < M.nnode; ++n) {
+    if (!M.submerged[n]) continue;
+    const double* xp = &M.g_coord[(size_t)3 * n];
+    bool next_node = false;
+    for (int w = 0; w < nwsurf && !next_node; ++w) {
+      const WaterSurf& S = ws[w];
+      if (S.stype == 0) {
+        double z = S.z1;
+        if (xp[S.rdir - 1] >= S.rx1 && xp[S.rdir - 1] <= S.rx2 && xp[2] <= z) {
+          if (z > xp[2]) M.wpressure[n] = gamw * (z - xp[2]);
+          next_node = true;
+        }
+      } else if (S.stype == 1) {
+        if (xp[S.rdir - 1] >= std::min(S.rx1, S.rx2) && xp[S.rdir - 1] <= std::max(S.rx1, S.rx2) &&
+            xp[2] <= std::max(S.z1, S.z2)) {
+          double z = S.z1 + (S.z2 - S.z1) * (xp[S.rdir - 1] - S.rx1) / (S.rx2 - S.rx1);
+          if (z > xp[2]) M.wpressure[n] = gamw * (z - xp[2]);
+          next_node = true;
+        }
+      } else if (S.stype == 2) {
+        for (size_t f = 0; f < S.ielmt.size() && !next_node; ++f) {
+          // face corners hexface(iface)%gnode = node(1), node(3), node(9), node(7)
+          const std::vector<int>& fn = T.face_nodes[S.iface[f] - 1];
+          const int corner[4] = {fn[0], fn[2], fn[8], fn[6]};
+          double xf[3][4];
+          for (int k = 0; k < 4; ++k)
+            for (int c = 0; c < 3; ++c)
+              xf[c][k] = M.g_coord[(size_t)3 * M.g_num[(size_t)(S.ielmt[f] - 1) * NGLL + corner[k]] + c];
+          double xmin = std::min(std::min(xf[0][0], xf[0][1]), std::min(xf[0][2], xf[0][3]));
+          double xmax = std::max(std::max(xf[0][0], xf[0][1]), std::max(xf[0][2], xf[0][3]));
+          double ymin = std::min(std::min(xf[1][0], xf[1][1]), std::min(xf[1][2], xf[1][3]));
+          double ymax = std::max(std::max(xf[1][0], xf[1][1]), std::max(xf[1][2], xf[1][3]));
+          double zmin = std::min(std::min(xf[2][0], xf[2][1]), std::min(xf[2][2], xf[2][3]));
+          double zmax = std::max(std::max(xf[2][0], xf[2][1]), std::max(xf[2][2], xf[2][3]));
+          if (!(xp[0] >= xmin && xp[0] <= xmax && xp[1] >= ymin && xp[1] <= ymax && xp[2] <= zmax)) continue;
+          double v1[3], v2[3];
+          for (int c = 0; c < 3; ++c) { v1[c] = xf[c][1] - xf[c][0]; v2[c] = xf[c][2] - xf[c][0]; }
+          double A = v1[1] * v2[2] - v2[1] * v1[2];
+          double B = v2[0] * v1[2] - v1[0] * v2[2];
+          double C = v1[0] * v2[1] - v2[0] * v1[1];
+          double m3[3][3];
+          for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) m3[r][c] = xf[r][c];
+          double D = determinant3(m3);  // as written in the reference (z = -(Ax+By+D)/C)
+          double z;
+          if (C == ZERO) {
+            std::fprintf(stderr, "WARNING: free surface face is vertical!\n");
+            z = zmax;
+          } else {
+            z = -(A * xp[0] + B * xp[1] + D) / C;
+          }
+          if (z > zmax || z < zmin) { errtag = "ERROR: free surface cannot be determined!"; return -1; }
+          if (z > xp[2]) M.wpressure[n] = gamw * (z - xp[2]);
+          next_node = true;
+        }
+      }
+    }
+  }
+  M.iswater = true;
+  return 0;
 }
 
 // gdof_elmt = reshape(gdof(:,g_num(:,e)),(/nedof/)) (src/slope.F90:140-144)
@@ -682,7 +784,7 @@ double stress_update(const Model& M, const int* elist, int nel, const double* x,
                      const int* gdof_elmt, const double* ymf, const double* nuf,
                      const double* phif, const double* cohf, const double* psif, double dt,
                      bool nl_isconv, bool finalize, double* evpt, double* stress_elmt,
-                     double* bodyload, double* vmeps, double* scf) {
+                     double* bodyload, double* vmeps, double* scf, bool wp_first = false) {
   const Tables& T = tables();
   double fmax = 0.0;
   const double r3 = 3.0, two_third = TWO / r3;
@@ -713,7 +815,21 @@ double stress_update(const Model& M, const int* elist, int nel, const double* x,
         for (int t = 0; t < 6; ++t) acc = acc + cmat[s][t] * eps[t];
         sigma[s] = acc;
       }
-      for (int s = 0; s < 6; ++s) eff[s] = sigma[s] + se[s];
+      // effective stress: slope3d adds the pore pressure of submerged nodes
+      // after the stored stress (src/slope.F90:334-341), excavation3d before it
+      // (src/excavation.F90:566-576)
+      const int nd_i = M.g_num[(size_t)e * NGLL + i];
+      const bool wet = M.iswater && M.submerged[nd_i];
+      if (wp_first) {
+        for (int s = 0; s < 6; ++s) eff[s] = sigma[s];
+        if (wet)
+          for (int s = 0; s < 3; ++s) eff[s] = eff[s] + M.wpressure[nd_i];
+        for (int s = 0; s < 6; ++s) eff[s] = eff[s] + se[s];
+      } else {
+        for (int s = 0; s < 6; ++s) eff[s] = sigma[s] + se[s];
+        if (wet)
+          for (int s = 0; s < 3; ++s) eff[s] = eff[s] + M.wpressure[nd_i];
+      }
       double sigm, dsbar, theta;
       stress_invariant(eff, sigm, dsbar, theta);
       double f = mohcouf(phif[imat], cohf[imat], sigm, dsbar, theta);
@@ -1057,6 +1173,18 @@ void* orc_model_from_deck(const char* path) {
     ss >> id >> dom >> typ;
     for (int k = 0; k < 6; ++k) ss >> props[6 * i + k];
   }
+  // water IDs after the material blocks (src/read_input.f90:602-611)
+  std::vector<char> water(nmat, 0);
+  const bool iswater = D.lines.count("water:") != 0;
+  if (iswater) {
+    int nwmat = 0;
+    fm >> nwmat;
+    for (int i = 0; i < nwmat; ++i) {
+      int id;
+      fm >> id;
+      water[id - 1] = 1;
+    }
+  }
   std::vector<int> counts(3, 0), pairs;
   const char* bck[3] = {"uxfile", "uyfile", "uzfile"};
   for (int d = 0; d < 3; ++d) {
@@ -1099,10 +1227,41 @@ void* orc_model_from_deck(const char* path) {
     C.eqky = eq.count("eqky") ? std::atof(eq["eqky"].c_str()) : 0.0;
     C.eqkz = eq.count("eqkz") ? std::atof(eq["eqkz"].c_str()) : 0.0;
   }
+  if (iswater) {  // src/slope.F90:173-187
+    std::string tag;
+    if (compute_pressure(h->M, water, base + D.lines["water:"]["wsfile"], tag) != 0) {
+      delete h;
+      return nullptr;
+    }
+  }
   return h;
 }
 
 void orc_free(void* h) { delete (OrcModel*)h; }
+
+// Water table: water_ids (1-based, nwmat) and a water-surface file
+// (src/compute_pressure.f90:10-186).  Returns 0, or -1 with errtag (250 chars).
+int orc_set_water(void* hv, const int* water_ids, int nwmat, const char* wsfile, char* errtag) {
+  OrcModel* h = (OrcModel*)hv;
+  std::vector<char> water(h->M.nmatblk, 0);
+  for (int i = 0; i < nwmat; ++i) water[water_ids[i] - 1] = 1;
+  std::string tag;
+  int st = compute_pressure(h->M, water, wsfile, tag);
+  if (errtag) std::snprintf(errtag, 250, "%s", tag.c_str());
+  return st;
+}
+
+// Pore pressure per node and submerged flags (either may be NULL).
+// Returns 0 when a water table is set, else -1.
+int orc_pore_pressure(void* hv, double* wpressure, int* submerged) {
+  OrcModel* h = (OrcModel*)hv;
+  if (!h->M.iswater) return -1;
+  for (int n = 0; n < h->M.nnode; ++n) {
+    if (wpressure) wpressure[n] = h->M.wpressure[n];
+    if (submerged) submerged[n] = h->M.submerged[n];
+  }
+  return 0;
+}
 
 // Valency-averaged nodal stress (src/slope.F90:419-437): stress_global(:,num) +=
 // stress_elmt(:,:,e) over the elements in order, then divided by node_valency.
@@ -1416,7 +1575,7 @@ int orc_excavation(void* hv, int s0_type, double z0, double s0, double k0, int n
         bool fin = nl_isconv || nl_iter == C.nl_maxiter;
         fmax = stress_update(M, eint.data(), nelmt_intact, x.data(), M.gdof_elmt.data(), M.ym.data(), nuf.data(),
                              phif.data(), cohf.data(), psif.data(), dt, nl_isconv, fin, evpt.data(), stress.data(),
-                             bodyload.data(), vmeps.data(), scf.data());
+                             bodyload.data(), vmeps.data(), scf.data(), true);
         if (fin) break;
       }
       if (errcode != 0) break;

@@ -35,7 +35,8 @@ PREC_FP64, PREC_MIXED = 0, 1
 EXPORTED = (
     "sg_create", "sg_create_status", "sg_destroy", "sg_last_error", "sg_hbm_used", "sg_pcg_solve",
     "sg_model_from_hex8", "sg_model_from_deck", "sg_model_free", "sg_model_info", "sg_model_arrays",
-    "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_nodal_stress", "sg_excavation_fields",
+    "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_model_set_water", "sg_model_set_pore_pressure",
+    "sg_model_pore_pressure", "sg_nodal_stress", "sg_excavation_fields",
     "sg_principal_stress", "sg_write_summary_header", "sg_write_summary_row", "sg_write_ensight_case", "sg_write_ensight_geo",
     "sg_write_ensight_var", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
@@ -139,6 +140,12 @@ def lib(path: Optional[str] = None):
     L.sg_write_ensight_var.argtypes = [C.c_char_p, C.c_char_p, i, i, vp]
     L.sg_model_set_eqload.restype = i
     L.sg_model_set_eqload.argtypes = [vp, d, d, d]
+    L.sg_model_set_water.restype = i
+    L.sg_model_set_water.argtypes = [vp, C.c_char_p, vp, i, C.c_char_p]
+    L.sg_model_set_pore_pressure.restype = i
+    L.sg_model_set_pore_pressure.argtypes = [vp, vp]
+    L.sg_model_pore_pressure.restype = i
+    L.sg_model_pore_pressure.argtypes = [vp, vp]
     L.sg_last_stress.restype = i
     L.sg_last_stress.argtypes = [vp, i, vp]
     L.sg_srf_sweep.restype = i
@@ -385,6 +392,34 @@ class Model:
         st = lib().sg_model_set_eqload(self.h, eqkx, eqky, eqkz)
         if st:
             raise SgError(st, self.ctx.last_error)
+
+    def set_water(self, water_ids: Sequence[int], wsfile: str):
+        """Water table: the water materials (1-based IDs) and a water-surface file
+        (the deck's water: line); the pore pressure is computed on the device."""
+        ids = np.ascontiguousarray(np.asarray(water_ids, np.int32).reshape(-1))
+        tag = C.create_string_buffer(ERRTAG_LEN + 1)
+        st = lib().sg_model_set_water(self.h, str(wsfile).encode(), _ptr(ids) if ids.size else None,
+                                      int(ids.size), tag)
+        if st:
+            raise SgError(st, tag.value.decode().strip())
+
+    def set_pore_pressure(self, wpressure):
+        """Pore pressure per node (nnode values); None removes it."""
+        if wpressure is None:
+            st = lib().sg_model_set_pore_pressure(self.h, None)
+        else:
+            wp = np.ascontiguousarray(wpressure, np.float64).reshape(-1)
+            if wp.size != self.nnode:
+                raise ValueError("wpressure needs one value per node")
+            st = lib().sg_model_set_pore_pressure(self.h, _ptr(wp))
+        if st:
+            raise SgError(st, self.ctx.last_error)
+
+    def pore_pressure(self):
+        """Pore pressure per node, or None when no water table is set."""
+        out = np.zeros(self.nnode)
+        st = lib().sg_model_pore_pressure(self.h, _ptr(out))
+        return None if st else out
 
     def trials(self, srf: Sequence[float], ctl: Control, want_x: bool = False):
         srf = np.ascontiguousarray(srf, np.float64)

@@ -6,6 +6,7 @@
 // element computation of the solve runs in the kernels of sg_kernels.cu.
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -594,6 +595,7 @@ struct sg_model {
   std::vector<double> last_stress_ok;
   std::vector<double> ex_vmeps, ex_scf;  // nodal fields of the last excavation stage
   double* d_fpart = nullptr;
+  double* d_wp = nullptr;  // pore pressure per node (water table set), else null
 };
 
 static void model_release_work(sg_model* M) {
@@ -765,6 +767,8 @@ sg_model* sg_model_from_hex8(sg_ctx* c, int nnode8, const double* x8, const doub
   return model_build(c, std::move(H), nnode8, x8, y8, z8, conn8, bc_counts, bc_pairs, precision, errtag);
 }
 
+static int model_set_water(sg_model* M, const std::string& wsfile, const int* water_ids, int nwmat, char* errtag);
+
 sg_model* sg_model_from_deck(sg_ctx* c, const char* path, int precision, char* errtag) {
   set_tag(errtag, "ERROR: unknown!");
   if (!c || !path) return nullptr;
@@ -781,8 +785,107 @@ sg_model* sg_model_from_deck(sg_ctx* c, const char* path, int precision, char* e
     H.gam.push_back(props[6 * i + 0]); H.ym.push_back(props[6 * i + 1]); H.nu.push_back(props[6 * i + 2]);
     H.phi.push_back(props[6 * i + 3]); H.coh.push_back(props[6 * i + 4]); H.psi.push_back(props[6 * i + 5]);
   }
-  return model_build(c, std::move(H), (int)x8.size(), x8.data(), y8.data(), z8.data(), conn.data(), cnt.data(),
-                     pairs.data(), precision, errtag);
+  const bool water = H.iswater != 0;
+  const std::string wsfile = H.wsfile;
+  const std::vector<int> wids = H.water_ids;
+  sg_model* M = model_build(c, std::move(H), (int)x8.size(), x8.data(), y8.data(), z8.data(), conn.data(),
+                            cnt.data(), pairs.data(), precision, errtag);
+  if (M && water) {
+    // pore pressure of the deck's water table (src/slope.F90:173-187)
+    int st = model_set_water(M, wsfile, wids.data(), (int)wids.size(), errtag);
+    if (st != SG_OK) { sg_model_free(M); return nullptr; }
+  }
+  return M;
+}
+
+// compute_pressure (src/compute_pressure.f90:10-186) on the device for the
+// surfaces of a water-surface file and the given water materials; the result
+// stays on the device as the model's pore pressure.
+static int model_set_water(sg_model* M, const std::string& wsfile, const int* water_ids, int nwmat, char* errtag) {
+  const HostMesh& h = M->H;
+  std::vector<WaterSurface> surf;
+  std::vector<int> face;
+  std::string err;
+  if (!read_wsfile(wsfile, h.nelmt, surf, face, err)) { set_tag(errtag, err); return SG_ERR_BADARG; }
+  std::vector<int> wm(h.nmatblk, 0);
+  for (int i = 0; i < nwmat; ++i) {
+    if (water_ids[i] < 1 || water_ids[i] > h.nmatblk) {
+      set_tag(errtag, "ERROR: water IDs must be consistent with the defined material regions!");
+      return SG_ERR_BADARG;
+    }
+    wm[water_ids[i] - 1] = 1;
+  }
+  sg_ctx* c = M->ctx;
+  cudaStream_t s = c->stream;
+  if (!M->d_wp) M->d_wp = c->alloc<double>(h.nnode);
+  WaterSurface* d_surf = c->alloc<WaterSurface>(surf.size() + 1);
+  int* d_face = c->alloc<int>(face.size() + 2);
+  int* d_wm = c->alloc<int>(wm.size() + 1);
+  int* d_sub = c->alloc<int>(h.nnode);
+  int* d_flag = c->alloc<int>(2);
+  int st = SG_OK;
+  if (!M->d_wp || !d_surf || !d_face || !d_wm || !d_sub || !d_flag) {
+    set_tag(errtag, "ERROR: out of device memory!");
+    st = SG_ERR_OOM;
+  } else {
+    cudaMemcpyAsync(d_surf, surf.data(), sizeof(WaterSurface) * surf.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_face, face.data(), sizeof(int) * face.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_wm, wm.data(), sizeof(int) * wm.size(), cudaMemcpyHostToDevice, s);
+    const int flag0[2] = {INT_MAX, 0};  // smallest failing node + 1 (atomicMin), vertical-face count
+    cudaMemcpyAsync(d_flag, flag0, sizeof(int) * 2, cudaMemcpyHostToDevice, s);
+    launch_water_pressure(h.nnode, h.nelmt, M->d_coord, M->d_gnum, M->d_matid, d_wm, d_surf, (int)surf.size(), d_face,
+                          d_sub, M->d_wp, d_flag, d_flag + 1, s);
+    int flag[2] = {0, 0};
+    cudaMemcpyAsync(flag, d_flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, s);
+    if (!c->check(cudaStreamSynchronize(s), "water pressure")) {
+      set_tag(errtag, "ERROR: CUDA error in the water pressure!");
+      st = SG_ERR_CUDA;
+    } else if (flag[0] != INT_MAX) {
+      set_tag(errtag, "ERROR: free surface cannot be determined!");
+      st = SG_ERR_BADARG;
+    } else if (flag[1]) {
+      std::fprintf(stderr, "WARNING: free surface face is vertical! (%d nodes)\n", flag[1]);
+    }
+  }
+  for (void* p : {(void*)d_surf, (void*)d_face, (void*)d_wm, (void*)d_sub, (void*)d_flag}) c->release(p);
+  if (st != SG_OK) { c->release(M->d_wp); M->d_wp = nullptr; }
+  return st;
+}
+
+int sg_model_set_water(sg_model* M, const char* wsfile, const int* water_ids, int nwmat, char* errtag) {
+  set_tag(errtag, "ERROR: unknown!");
+  if (!M || !wsfile || nwmat < 0 || (nwmat > 0 && !water_ids) || M->B.open) return SG_ERR_BADARG;
+  int st = model_set_water(M, wsfile, water_ids, nwmat, errtag);
+  if (st == SG_OK) {
+    M->H.iswater = 1;
+    M->H.wsfile = wsfile;
+    M->H.water_ids.assign(water_ids, water_ids + nwmat);
+  }
+  return st;
+}
+
+int sg_model_set_pore_pressure(sg_model* M, const double* wpressure) {
+  if (!M || M->B.open) return SG_ERR_BADARG;
+  sg_ctx* c = M->ctx;
+  if (!wpressure) {
+    cudaStreamSynchronize(c->stream);
+    c->release(M->d_wp);
+    M->d_wp = nullptr;
+    M->H.iswater = 0;
+    return SG_OK;
+  }
+  if (!M->d_wp) M->d_wp = c->alloc<double>(M->H.nnode);
+  if (!M->d_wp) return SG_ERR_OOM;
+  cudaMemcpyAsync(M->d_wp, wpressure, sizeof(double) * M->H.nnode, cudaMemcpyHostToDevice, c->stream);
+  M->H.iswater = 1;
+  return c->check(cudaStreamSynchronize(c->stream), "pore pressure") ? SG_OK : SG_ERR_CUDA;
+}
+
+int sg_model_pore_pressure(const sg_model* M, double* wpressure) {
+  if (!M || !wpressure || !M->d_wp) return SG_ERR_BADARG;
+  sg_ctx* c = M->ctx;
+  cudaMemcpyAsync(wpressure, M->d_wp, sizeof(double) * M->H.nnode, cudaMemcpyDeviceToHost, c->stream);
+  return c->check(cudaStreamSynchronize(c->stream), "pore pressure") ? SG_OK : SG_ERR_CUDA;
 }
 
 void sg_model_free(sg_model* M) {
@@ -795,7 +898,7 @@ void sg_model_free(sg_model* M) {
   for (void* p : {(void*)M->d_coord, (void*)M->d_gnum, (void*)M->d_matid, (void*)M->d_ge, (void*)M->d_gdof,
                   (void*)M->d_ym, (void*)M->d_nu, (void*)M->d_gam, (void*)M->d_geo, (void*)M->d_K64, (void*)M->d_K32,
                   (void*)M->d_rec32, (void*)M->d_diag, (void*)M->d_dprecon, (void*)M->d_extload, (void*)M->d_dprecon32,
-                  (void*)M->d_Yscratch, (void*)M->d_fpart})
+                  (void*)M->d_Yscratch, (void*)M->d_fpart, (void*)M->d_wp})
     c->release(p);
   delete M;
 }
@@ -1169,7 +1272,8 @@ static int batch_iteration(sg_model* M) {
     fin[t] = conv[t] || S.res.nl_iter == ctl->nl_maxiter;
     int ev = c->prof_begin();
     launch_stress_update(M->d_geo, nullptr, ne, M->d_ge, M->d_matid, W.x, KR, t, W.mf + (size_t)t * h.nmatblk, S.dt,
-                         conv[t], fin[t], W.evpt + nst * t, W.stress + nst * t, W.Yb, KR, t, M->d_fpart, M->T.d_pos, s);
+                         conv[t], fin[t], W.evpt + nst * t, W.stress + nst * t, W.Yb, KR, t, M->d_fpart, M->T.d_pos, s,
+                         nullptr, nullptr, M->d_wp, M->d_gnum, 0);
     c->prof_end(ev, 4);
     reduce_read(c, M->d_fpart, NPART, 1, 1, 1, W.red, red + 32);
     S.res.fmax = red[32];
@@ -1523,7 +1627,7 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
             double uerr = red[0] / red[1];
             int conv = uerr <= ctl->nl_tol, fin = conv || nl_iter == ctl->nl_maxiter;
             launch_stress_update(M->d_geo, d_eint, nint, d_geall, M->d_matid, W.x, 1, 0, W.mf, dt, conv, fin, evpt,
-                                 stress, W.Yb, 1, 0, M->d_fpart, Ti.d_pos, s, d_vm, d_sf);
+                                 stress, W.Yb, 1, 0, M->d_fpart, Ti.d_pos, s, d_vm, d_sf, M->d_wp, M->d_gnum, 1);
             reduce_read(c, M->d_fpart, NPART, 1, 1, 1, W.red, red);
             fmax = red[0];
             if (!fin) launch_gather_plain<double>(Ti, 1, W.Yb, W.bodyload, 1, nullptr, s);

@@ -229,7 +229,7 @@ const KsTables& ks_tables() {
 
 // ---------------------------------------------------------------------------
 // .sem deck reader: the subset of src/read_input.f90:13-619 the solve path
-// uses (preinfo, mesh, bc, material, control, stress0, eqload; save/water/
+// uses (preinfo, mesh, bc, material, control, stress0, eqload, water; save and
 // traction lines are accepted and ignored).  File names resolve relative to the
 // deck's directory.  Defaults: cg_tol = nl_tol = 1e-12, cg_maxiter =
 // nl_maxiter = 100 (src/read_input.f90:109-110).
@@ -336,6 +336,15 @@ bool read_deck(const char* path, HostMesh& M, std::vector<double>& x8, std::vect
     M.allelastic = mat.count("allelastic") && std::atoi(mat["allelastic"].c_str()) == 1;
     for (int m : mid)
       if (m < 1 || m > M.nmatblk) { err = "ERROR: material IDs must be consistent with the defined material regions!"; return false; }
+    if (L.count("water:")) {  // src/read_input.f90:307-317 and 602-611
+      M.iswater = 1;
+      M.wsfile = base + L["water:"]["wsfile"];
+      int nwmat;
+      if (!(f >> nwmat)) { err = "ERROR: water IDs cannot be read from material list!"; return false; }
+      M.water_ids.resize(nwmat > 0 ? nwmat : 0);
+      for (auto& id : M.water_ids)
+        if (!(f >> id) || id < 1 || id > M.nmatblk) { err = "ERROR: water IDs cannot be read from material list!"; return false; }
+    }
   }
   bc_counts.assign(3, 0);
   bc_pairs.clear();
@@ -410,6 +419,50 @@ bool read_deck(const char* path, HostMesh& M, std::vector<double>& x8, std::vect
     M.eqkz = eq.count("eqkz") ? std::atof(eq["eqkz"].c_str()) : 0.0;
   }
   (void)nnode8;
+  return true;
+}
+
+// Water-surface file (src/compute_pressure.f90:55-86), list-directed: nwsurf,
+// then per surface its kind and, by kind, "rdir rx1 rx2 z1" (0),
+// "rdir rx1 rx2 z1 z2" (1) or "nface" followed by nface "ielmt iface" lines (2).
+bool read_wsfile(const std::string& path, int nelmt, std::vector<WaterSurface>& surf, std::vector<int>& face,
+                 std::string& err) {
+  std::ifstream in(path);
+  if (!in) { err = "ERROR: input file \"" + path + "\" cannot be opened!"; return false; }
+  std::stringstream ss;
+  {
+    std::string all((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+    for (char& ch : all) if (ch == ',') ch = ' ';
+    ss.str(all);
+  }
+  int nw;
+  if (!(ss >> nw) || nw < 0) { err = "ERROR: bad water-surface file!"; return false; }
+  surf.assign(nw, WaterSurface{0, 1, 0, 0, 0.0, 0.0, 0.0, 0.0});
+  face.clear();
+  for (auto& w : surf) {
+    if (!(ss >> w.stype)) { err = "ERROR: bad water-surface file!"; return false; }
+    bool ok = true;
+    if (w.stype == 0) ok = bool(ss >> w.rdir >> w.rx1 >> w.rx2 >> w.z1);
+    else if (w.stype == 1) ok = bool(ss >> w.rdir >> w.rx1 >> w.rx2 >> w.z1 >> w.z2);
+    else if (w.stype == 2) {
+      ok = bool(ss >> w.nface) && w.nface >= 0;
+      w.face0 = (int)face.size() / 2;
+      for (int f = 0; ok && f < w.nface; ++f) {
+        int e, fc;
+        ok = bool(ss >> e >> fc) && e >= 1 && e <= nelmt && fc >= 1 && fc <= 6;
+        face.push_back(e - 1);
+        face.push_back(fc);
+      }
+    } else {
+      // the reference reads no parameters for other kinds and never matches them
+      w.nface = 0;
+      w.stype = 3;
+    }
+    if (!ok || ((w.stype == 0 || w.stype == 1) && (w.rdir < 1 || w.rdir > 3))) {
+      err = "ERROR: bad water-surface file!";
+      return false;
+    }
+  }
   return true;
 }
 

@@ -67,7 +67,20 @@ struct HostMesh {
   double z0 = 0, s0 = 0, k0 = 0;
   int iseqload = 0;                       // pseudo-static load (eqload: line)
   double eqkx = 0, eqky = 0, eqkz = 0;
+  int iswater = 0;                        // water: line
+  std::string wsfile;                     // water-surface file, resolved against the deck's directory
+  std::vector<int> water_ids;             // 1-based water material IDs (material list tail)
 };
+
+// One record of a water-surface file (src/compute_pressure.f90:61-86): kind 0
+// horizontal line, 1 inclined line, 2 meshed faces, the latter listed as
+// (0-based element, Exodus face) pairs face[2*(face0+f)], f < nface.
+struct WaterSurface {
+  int stype, rdir, face0, nface;
+  double rx1, rx2, z1, z2;
+};
+bool read_wsfile(const std::string& path, int nelmt, std::vector<WaterSurface>& surf, std::vector<int>& face,
+                 std::string& err);
 
 // host mesh construction (sg_host_mesh.cu)
 bool hex2spec(HostMesh& M, int nnode8, const double* x8, const double* y8, const double* z8,

@@ -1426,7 +1426,8 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
     const int* __restrict__ mat_id, const double* __restrict__ x, int xstride, int xcol, const MatF* __restrict__ mf,
     double dt, int nl_isconv, int finalize, double* __restrict__ evpt, double* __restrict__ stress,
     double* __restrict__ Yb, int ystride, int ycol, double* __restrict__ fmax_part, const int* __restrict__ pos,
-    double* __restrict__ vm_pt, double* __restrict__ sf_pt) {
+    double* __restrict__ vm_pt, double* __restrict__ sf_pt, const double* __restrict__ wp,
+    const int* __restrict__ gnum, int wp_first) {
   __shared__ double s_eld[STRESS_WARPS][NEDOF];
   __shared__ double s_q[STRESS_WARPS][NGLL][9];
   __shared__ double s_fmax[STRESS_WARPS];
@@ -1477,9 +1478,23 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
       sig[1] = m.c12 * eps[0] + m.c11 * eps[1] + m.c12 * eps[2];
       sig[2] = m.c12 * eps[0] + m.c12 * eps[1] + m.c11 * eps[2];
       sig[3] = m.c44 * eps[3]; sig[4] = m.c44 * eps[4]; sig[5] = m.c44 * eps[5];
+      // effective stress; the pore pressure p of the point's node (0 off the
+      // submerged nodes) is added to the normal components, after the stored
+      // stress in the slope form (src/slope.F90:334-341) and before it in the
+      // excavation form (src/excavation.F90:566-576)
       double eff[6];
+      if (wp) {
+        const double pw = wp[gnum[(size_t)e * NGLL + i]];
 #pragma unroll
-      for (int s = 0; s < 6; ++s) eff[s] = sig[s] + se[s];
+        for (int s = 0; s < 6; ++s) {
+          if (s >= 3) eff[s] = sig[s] + se[s];
+          else if (wp_first) eff[s] = (sig[s] + pw) + se[s];
+          else eff[s] = (sig[s] + se[s]) + pw;
+        }
+      } else {
+#pragma unroll
+        for (int s = 0; s < 6; ++s) eff[s] = sig[s] + se[s];
+      }
       double sigm, dsbar, theta;
       stress_invariant_d(eff, sigm, dsbar, theta);
       double snth, csth;
@@ -1618,11 +1633,121 @@ __global__ void __launch_bounds__(STRESS_WARPS * 32) k_stress_update(
 void launch_stress_update(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
                           const double* x, int xstride, int xcol, const MatF* mf, double dt, int nl_isconv,
                           int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
-                          double* fmax_part, const int* pos, cudaStream_t s, double* vm_pt, double* sf_pt) {
+                          double* fmax_part, const int* pos, cudaStream_t s, double* vm_pt, double* sf_pt,
+                          const double* wp, const int* gnum, int wp_first) {
   // fixed grid so that fmax_part has NPART entries
   SG_LAUNCH k_stress_update<<<NPART, STRESS_WARPS * 32, 0, s>>>(geo, elist, nel, ge_glob, mat_id, x, xstride, xcol, mf, dt,
                                                        nl_isconv, finalize, evpt, stress, Yb, ystride, ycol,
-                                                       fmax_part, pos, vm_pt, sf_pt);
+                                                       fmax_part, pos, vm_pt, sf_pt, wp, gnum, wp_first);
+}
+
+// ---------------------------------------------------------------------------
+// compute_pressure (src/compute_pressure.f90:10-186): hydrostatic pressure
+// gamw (z - z_node) under a water table, on the nodes of the elements whose
+// material is a water material.  k_mark_submerged flags those nodes;
+// k_water_pressure gives each node one thread that scans the surfaces in file
+// order and stops at the first one the node lies under (the reference's
+// `cycle nodal`).  Surface kinds: 0 horizontal line z1 over rdir in [rx1, rx2];
+// 1 inclined line z1 -> z2 over rdir in [min(rx1,rx2), max(rx1,rx2)];
+// 2 meshed faces, with the reference's plane offset D = det[xf1 xf2 xf3] taken
+// as it is written (z = -(A x + B y + D)/C), a vertical face taking its top z,
+// and a z outside the face's z range stopping the computation with an error
+// (err, INT_MAX on entry, receives the smallest failing node + 1); nvert counts
+// vertical faces met.
+// ---------------------------------------------------------------------------
+__global__ void k_mark_submerged(const int* __restrict__ g_num, const int* __restrict__ mat_id,
+                                 const int* __restrict__ water_mat, int nelmt, int* __restrict__ sub) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nelmt * NGLL) return;
+  if (water_mat[mat_id[t / NGLL] - 1]) sub[g_num[t]] = 1;
+}
+
+// corner nodes (0-based GLL numbering) of Exodus faces 1..6, the reference's
+// hexface(:)%gnode for NGLL = 3 (src/element.f90:107-124)
+__constant__ int c_face_corner[6][4] = {{0, 2, 20, 18}, {2, 8, 26, 20}, {6, 8, 26, 24},
+                                        {0, 6, 24, 18}, {0, 2, 8, 6},   {18, 20, 26, 24}};
+
+__global__ void k_water_pressure(int nnode, const double* __restrict__ g_coord, const int* __restrict__ sub,
+                                 const WaterSurface* __restrict__ surf, int nsurf, const int* __restrict__ face,
+                                 const int* __restrict__ g_num, double* __restrict__ wp, int* __restrict__ err,
+                                 int* __restrict__ nvert) {
+  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= nnode) return;
+  const double gamw = 9.81;
+  double p = 0.0;
+  if (sub[n]) {
+    const double xp[3] = {g_coord[3 * (size_t)n], g_coord[3 * (size_t)n + 1], g_coord[3 * (size_t)n + 2]};
+    bool done = false;
+    for (int w = 0; w < nsurf && !done; ++w) {
+      const WaterSurface S = surf[w];
+      if (S.stype == 0) {
+        const double r = xp[S.rdir - 1], z = S.z1;
+        if (r >= S.rx1 && r <= S.rx2 && xp[2] <= z) {
+          if (z > xp[2]) p = gamw * (z - xp[2]);
+          done = true;
+        }
+      } else if (S.stype == 1) {
+        const double r = xp[S.rdir - 1];
+        if (r >= fmin(S.rx1, S.rx2) && r <= fmax(S.rx1, S.rx2) && xp[2] <= fmax(S.z1, S.z2)) {
+          const double z = S.z1 + (S.z2 - S.z1) * (r - S.rx1) / (S.rx2 - S.rx1);
+          if (z > xp[2]) p = gamw * (z - xp[2]);
+          done = true;
+        }
+      } else {
+        for (int f = 0; f < S.nface && !done; ++f) {
+          const int e = face[2 * (S.face0 + f)], fc = face[2 * (S.face0 + f) + 1];
+          double xf[3][4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int nd = g_num[(size_t)e * NGLL + c_face_corner[fc - 1][k]];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) xf[c][k] = g_coord[3 * (size_t)nd + c];
+          }
+          double lo[3], hi[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            lo[c] = fmin(fmin(xf[c][0], xf[c][1]), fmin(xf[c][2], xf[c][3]));
+            hi[c] = fmax(fmax(xf[c][0], xf[c][1]), fmax(xf[c][2], xf[c][3]));
+          }
+          if (!(xp[0] >= lo[0] && xp[0] <= hi[0] && xp[1] >= lo[1] && xp[1] <= hi[1] && xp[2] <= hi[2])) continue;
+          const double v1[3] = {xf[0][1] - xf[0][0], xf[1][1] - xf[1][0], xf[2][1] - xf[2][0]};
+          const double v2[3] = {xf[0][2] - xf[0][0], xf[1][2] - xf[1][0], xf[2][2] - xf[2][0]};
+          const double A = v1[1] * v2[2] - v2[1] * v1[2];
+          const double B = v2[0] * v1[2] - v1[0] * v2[2];
+          const double C = v1[0] * v2[1] - v2[0] * v1[1];
+          // determinant of the 3x3 matrix whose columns are the first three corners
+          const double D = xf[0][0] * (xf[1][1] * xf[2][2] - xf[2][1] * xf[1][2]) -
+                           xf[0][1] * (xf[1][0] * xf[2][2] - xf[2][0] * xf[1][2]) +
+                           xf[0][2] * (xf[1][0] * xf[2][1] - xf[2][0] * xf[1][1]);
+          double z;
+          if (C == 0.0) {
+            atomicAdd(nvert, 1);
+            z = hi[2];
+          } else {
+            z = -(A * xp[0] + B * xp[1] + D) / C;
+          }
+          if (z > hi[2] || z < lo[2]) {
+            atomicMin(err, n + 1);
+            return;
+          }
+          if (z > xp[2]) p = gamw * (z - xp[2]);
+          done = true;
+        }
+      }
+    }
+  }
+  wp[n] = p;
+}
+
+void launch_water_pressure(int nnode, int nelmt, const double* g_coord, const int* g_num, const int* mat_id,
+                           const int* water_mat, const WaterSurface* surf, int nsurf, const int* face, int* sub,
+                           double* wp, int* err, int* nvert, cudaStream_t s) {
+  cudaMemsetAsync(sub, 0, sizeof(int) * (size_t)nnode, s);
+  if (nelmt > 0)
+    SG_LAUNCH k_mark_submerged<<<(nelmt * NGLL + 255) / 256, 256, 0, s>>>(g_num, mat_id, water_mat, nelmt, sub);
+  if (nnode > 0)
+    SG_LAUNCH k_water_pressure<<<(nnode + 255) / 256, 256, 0, s>>>(nnode, g_coord, sub, surf, nsurf, face, g_num,
+                                                                  wp, err, nvert);
 }
 
 // elastic_stress (src/postprocess.f90:40-79): sigma = C B x per GLL point

@@ -94,7 +94,14 @@ void launch_stress_update(const double* geo, const int* elist, int nel, const in
                           const double* x, int xstride, int xcol, const MatF* mf, double dt, int nl_isconv,
                           int finalize, double* evpt, double* stress, double* Yb, int ystride, int ycol,
                           double* fmax_part, const int* pos, cudaStream_t s, double* vm_pt = nullptr,
-                          double* sf_pt = nullptr);
+                          double* sf_pt = nullptr, const double* wp = nullptr, const int* gnum = nullptr,
+                          int wp_first = 0);
+// submerged-node flags and hydrostatic pore pressure per node; err (set to
+// INT_MAX by the caller) gets the smallest node + 1 whose free surface cannot
+// be determined
+void launch_water_pressure(int nnode, int nelmt, const double* g_coord, const int* g_num, const int* mat_id,
+                           const int* water_mat, const WaterSurface* surf, int nsurf, const int* face, int* sub,
+                           double* wp, int* err, int* nvert, cudaStream_t s);
 void launch_elastic_stress(const double* geo, const int* elist, int nel, const int* ge_glob, const int* mat_id,
                            const double* x, int xstride, int xcol, const MatF* mf, int accumulate, double* stress,
                            cudaStream_t s);

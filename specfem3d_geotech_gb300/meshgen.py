@@ -66,6 +66,8 @@ class Hex8Mesh:
     control: Control
     name: str = "mesh"
     stress0: Optional[Tuple[int, float, float, float]] = None  # (type, z0, s0, k0)
+    # water table: (1-based water material IDs, text of the water-surface file)
+    water: Optional[Tuple[Tuple[int, ...], str]] = None
 
     @property
     def nelmt(self) -> int:
@@ -240,6 +242,18 @@ def column(n: int = 4, H: float = 4.0, E: float = 1e5, nu: float = 0.3, gam: flo
     return Hex8Mesh(x, y, z, conn, np.ones(n, np.int32), props, bc, ctl, name="column")
 
 
+def box(nx: int = 4, ny: int = 4, nz: int = 4, L: float = 4.0, W: float = 4.0, zbot: float = 0.0,
+        ztop: float = 4.0, props=(20.0, 1e5, 0.3, 30.0, 10.0, 0.0)) -> Hex8Mesh:
+    """Structured box [0, L] x [0, W] x [zbot, ztop] of nx*ny*nz elements
+    (element e = i + nx*(j + ny*k), 1-based in conn order), bottom fixed,
+    sides on rollers; one material (gamma, E, nu, phi, c, psi)."""
+    x, y, z, conn, ijk = _structured(nx, ny, nz, np.linspace(0.0, L, nx + 1), np.linspace(0.0, W, ny + 1),
+                                     lambda X, Y: np.full_like(X, ztop), zbot=zbot)
+    ctl = Control(cg_tol=1e-8, cg_maxiter=5000, nl_tol=1e-4, nl_maxiter=200, srf=(1.0,))
+    return Hex8Mesh(x, y, z, conn, np.ones(conn.shape[0], np.int32), np.array([props], np.float64),
+                    _box_bcs(ijk, nx, ny, nz), ctl, name="box")
+
+
 def write_deck(mesh: Hex8Mesh, directory: str, head: Optional[str] = None) -> str:
     """Write `mesh` as a reference-format serial deck (``<head>.sem`` + files)."""
     head = head or mesh.name
@@ -260,6 +274,13 @@ def write_deck(mesh: Hex8Mesh, directory: str, head: Optional[str] = None) -> st
         f.write(f"{mesh.props.shape[0]}\n")
         for i, p in enumerate(mesh.props):
             f.write(f"{i + 1}, 1, 0, " + ", ".join("%.17g" % v for v in p) + "\n")
+        if mesh.water is not None:  # water IDs follow the blocks (src/read_input.f90:602-611)
+            f.write(f"{len(mesh.water[0])}\n")
+            for wid in mesh.water[0]:
+                f.write(f"{wid}\n")
+    if mesh.water is not None:
+        with open(os.path.join(directory, f"{head}_water_surface"), "w") as f:
+            f.write(mesh.water[1])
     for d, nm in enumerate(("ssbcux", "ssbcuy", "ssbcuz")):
         with open(os.path.join(directory, f"{head}_{nm}"), "w") as f:
             f.write("2 0.0\n")
@@ -280,6 +301,8 @@ def write_deck(mesh: Hex8Mesh, directory: str, head: Optional[str] = None) -> st
         lines += ["#initial stress", f"stress0: type={t}, z0={z0:g}, s0={s0:g}, k0={k0:g}"]
     lines += ["#material list", f"material: matfile='{head}_material_list'" +
               (", allelastic=1" if c.allelastic else "")]
+    if mesh.water is not None:
+        lines += ["#water table", f"water: wsfile='{head}_water_surface'"]
     ctl = (f"control: cg_tol={c.cg_tol:g}, cg_maxiter={c.cg_maxiter}, nl_tol={c.nl_tol:g}, "
            f"nl_maxiter={c.nl_maxiter}, nsrf={len(c.srf)}, srf=" + " ".join("%g" % s for s in c.srf))
     if c.nexcav:

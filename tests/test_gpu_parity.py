@@ -487,3 +487,102 @@ def test_persistent_pcg_matches_separate_kernels(tmp_path, k):
     for t in range(k):
         assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
     assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
+
+
+def _ws(tmp_path, text, name="ws.txt"):
+    p = tmp_path / name
+    p.write_text(text)
+    return str(p)
+
+
+def test_water_pressure_matches_oracle(ctx, tmp_path):
+    """compute_pressure on the device (k_mark_submerged + k_water_pressure)
+    against the oracle for the line kinds, the first-surface rule and a meshed
+    surface; the deck's water: line gives the same field; a meshed surface off
+    the origin plane is the reference's error."""
+    slope2d = meshgen.slope2d(srf=(1.0,))
+    slope2d.props = np.vstack([slope2d.props, slope2d.props])
+    xc = slope2d.x[slope2d.conn - 1].mean(axis=1)
+    slope2d.mat_id = np.where(xc < 14.0, 2, 1).astype(np.int32)
+    box = meshgen.box(nx=3, ny=2, nz=3, L=3.0, W=2.0, zbot=-3.0, ztop=0.0)
+    top = [(i + 3 * (j + 2 * 2) + 1, meshgen.FACE_ZMAX) for j in range(2) for i in range(3)]
+    cases = [
+        (slope2d, [2], "2\n0\n1 0.0 10.0 2.0\n1\n1 0.0 20.0 3.0 7.0\n"),
+        (box, [1], "1\n2\n%d\n" % len(top) + "".join("%d %d\n" % f for f in top)),
+    ]
+    for n, (mesh, ids, text) in enumerate(cases):
+        path = _ws(tmp_path, text, f"ws{n}.txt")
+        om = OracleModel(mesh)
+        om.set_water(ids, path)
+        m = sg.Model(mesh, ctx=ctx)
+        assert m.pore_pressure() is None
+        m.set_water(ids, path)
+        wp_o, sub_o = om.pore_pressure()
+        wp = m.pore_pressure()
+        assert (wp_o > 0).sum() > 0
+        np.testing.assert_allclose(wp, wp_o, rtol=1e-13, atol=1e-12)
+        assert np.array_equal(wp[~sub_o], np.zeros((~sub_o).sum()))
+    mesh, ids, text = cases[0]
+    mesh.water = (tuple(ids), text)
+    deck = meshgen.write_deck(mesh, str(tmp_path / "deck"))
+    md = sg.Model(None, deck=deck, ctx=ctx)
+    od = OracleModel(deck=deck)
+    np.testing.assert_allclose(md.pore_pressure(), od.pore_pressure()[0], rtol=1e-13, atol=1e-12)
+    high = meshgen.box(nx=2, ny=2, nz=2, L=2.0, W=2.0, zbot=0.0, ztop=5.0)
+    faces = [(i + 2 * (j + 2) + 1, meshgen.FACE_ZMAX) for j in range(2) for i in range(2)]
+    path = _ws(tmp_path, "1\n2\n4\n" + "".join("%d %d\n" % f for f in faces), "high.txt")
+    mh = sg.Model(high, ctx=ctx)
+    with pytest.raises(sg.SgError, match="free surface cannot be determined"):
+        mh.set_water([1], path)
+    assert mh.pore_pressure() is None
+
+
+def test_water_trial_matches_oracle(ctx, tmp_path):
+    """A plastic slope trial under a water table (pore pressure added to the
+    effective stress after the stored stress, src/slope.F90:334-341) matches
+    the oracle's, in FP64 and in the mixed form."""
+    mesh = meshgen.slope2d(srf=(1.0,))
+    path = _ws(tmp_path, "1\n0\n1 0.0 20.0 6.0\n")
+    om = OracleModel(mesh)
+    om.set_water([1], path)
+    ro = om.trial(1.0, want_x=True, want_stress=True)
+    assert ro["converged"] == 1
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=2000)
+    m = sg.Model(mesh, ctx=ctx)
+    m.set_water([1], path)
+    (r,), x = m.trials([1.0], ctl, want_x=True)
+    assert r["nl_iter"] == ro["nl_iter"] and r["converged"] == 1
+    assert rel(x[0], ro["x"]) <= TRIAL_TOL
+    st = m.last_stress(0)
+    assert np.abs(st - ro["stress"]).max() <= STRESS_TOL * np.abs(ro["stress"]).max()
+    assert abs(r["fmax"] - ro["fmax"]) <= FMAX_TOL * abs(ro["fmax"])
+    mm = sg.Model(mesh, ctx=ctx, precision=sg.PREC_MIXED)
+    mm.set_water([1], path)
+    ctl32 = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=2000, precision=sg.PREC_MIXED)
+    (rm,), xm = mm.trials([1.0], ctl32, want_x=True)
+    assert rm["nl_iter"] == ro["nl_iter"]
+    assert rel(xm[0], ro["x"]) <= MIXED_TOL
+    # removing the pressure gives the dry trial back
+    m.set_pore_pressure(None)
+    (rd,), xd = m.trials([1.0], ctl, want_x=True)
+    rdo = OracleModel(mesh).trial(1.0, want_x=True)
+    assert rd["nl_iter"] == rdo["nl_iter"] and rel(xd[0], rdo["x"]) <= TRIAL_TOL
+
+
+def test_water_excavation_matches_oracle(ctx, tmp_path):
+    """Staged excavation under a water table (pore pressure added before the
+    stored stress, src/excavation.F90:566-576)."""
+    mesh = meshgen.excavation(nx=6, ny=6, nz=4, L=12.0, H=8.0, pit=4.0, lifts=2, lift_h=2.0)
+    path = _ws(tmp_path, "1\n0\n1 0.0 12.0 5.0\n")
+    om = OracleModel(mesh)
+    om.set_control(1e-8, 5000, 1e-4, 200)
+    om.set_water([1], path)
+    ro = om.excavation(1, 8.0, 0.0, 0.5, [2, 3])
+    m = sg.Model(mesh, ctx=ctx)
+    m.set_water([1], path)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=200)
+    r = m.excavation(ctl, 1, 8.0, 0.0, 0.5, [2, 3])
+    assert r.shape == ro.shape
+    assert ro[1, 2] > 2                                  # the water changes the second stage
+    assert np.array_equal(r[:, 2], ro[:, 2])
+    assert np.allclose(r[:, 3:5], ro[:, 3:5], rtol=1e-8)
