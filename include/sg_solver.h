@@ -68,6 +68,38 @@ int sg_pcg_solve(sg_ctx* ctx, int neq, int nelmt, int nedof, const double* k, do
                  const double* f, const double* dprecon, const int* gdof_elmt, int cg_maxiter,
                  double cg_tol, int* cg_iter, char* errtag);
 
+/* Replaces the stress / yield / viscoplastic-flow / body-load block that the
+ * plastic loops inline after each pcg_solver call: src/slope.F90:311-383, and
+ * its excavation copy src/excavation.F90:546-616.  With sg_pcg_solve it lets a
+ * host keep its own plastic loop and run both heavy steps on the GPU.  Arrays
+ * are the reference's own, ids 1-based:
+ *   g_coord[3*nnode], g_num[27*nelmt] (nodes 1..nnode, GLL order i+3j+9k),
+ *   gdof_elmt[81*nelmt] in [0,neq], mat_id[nelmt] in [1,nmatblk];
+ *   ym_blk and the factored nuf/phif/cohf/psif_blk[nmatblk] (angles in degrees,
+ *   src/plastic_library.f90:42-88), dt (src/plastic_library.f90:17-39);
+ *   elmt_list[nel]: elements 1..nelmt to visit in order (elmt_intact), or NULL
+ *   for all nelmt;
+ *   x[neq+1]; evpt and stress_elmt[6*27*nelmt] in/out;
+ *   bodyload[neq+1] in/out: the element loads are added in element order
+ *   unless last, and bodyload[0] is set to 0;
+ *   wpressure[nnode] or NULL: pore pressure added to the normal effective
+ *   stress (0 on nodes that are not submerged);
+ *   form 0: slope order (pressure after the stored stress);
+ *   form 1: excavation order (pressure before it), and when last, vmeps[nnode]
+ *   += the points' von Mises plastic strain and scf[nnode] = min(scf, point
+ *   safety factor) (either may be NULL);
+ *   last = nl_isconv .or. nl_iter == nl_maxiter: the stress is stored, no load.
+ * fmax receives max(0, max F) over the visited points.  The mesh, dof map,
+ * material ids and element list are uploaded only when they change between
+ * calls; the plastic state is copied in and out on every call. */
+int sg_stress_bodyload(sg_ctx* ctx, int neq, int nelmt, int nnode, const double* g_coord, const int* g_num,
+                       const int* gdof_elmt, const int* mat_id, int nmatblk, const double* ym_blk,
+                       const double* nuf_blk, const double* phif_blk, const double* cohf_blk,
+                       const double* psif_blk, double dt, int nl_isconv, int last, const int* elmt_list,
+                       int nel, const double* wpressure, int form, const double* x, double* evpt,
+                       double* stress_elmt, double* bodyload, double* vmeps, double* scf, double* fmax,
+                       char* errtag);
+
 /* No counterpart in the reference.  The same solve as sg_pcg_solve (same
  * arguments and results, host arrays in and out) for callers that cannot
  * allocate device memory -- code that runs under its own memory pool or

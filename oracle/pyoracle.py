@@ -56,7 +56,8 @@ def lib():
         L.orc_pcg_solver.argtypes = [i, i, _dp, _dp, _dp, _dp, _ip, i, d, C.POINTER(C.c_int)]
         L.orc_ebe_apply.argtypes = [i, i, _dp, _dp, _ip, _dp]
         L.orc_stress_update.restype = d
-        L.orc_stress_update.argtypes = [vp, _dp, _dp, _dp, _dp, _dp, _dp, d, i, i, _dp, _dp, _dp]
+        L.orc_stress_update.argtypes = [vp, vp, i, i, _dp, _dp, _dp, _dp, _dp, _dp, d, i, i, _dp, _dp, _dp, vp,
+                                        vp]
         L.orc_elastic_stress.argtypes = [vp, _dp, _dp]
         L.orc_overburden_stress.argtypes = [vp, d, d, d, _dp]
         L.orc_strength_reduction.restype = i
@@ -143,6 +144,19 @@ class OracleModel:
             return None
         return wp, sub.astype(bool)
 
+    def stress_update(self, x, ymf, nuf, phif, cohf, psif, dt, nl_isconv, last, evpt, stress, bodyload,
+                      elist=None, form=0, vmeps=None, scf=None):
+        """One pass of the stress / yield / flow / body-load block
+        (src/slope.F90:311-383, src/excavation.F90:546-616); evpt, stress,
+        bodyload (and vmeps, scf) are float64 arrays updated in place.
+        Returns fmax."""
+        el = None if elist is None else np.ascontiguousarray(elist, np.int32)
+        f = lambda a: np.ascontiguousarray(a, np.float64)
+        return lib().orc_stress_update(
+            self.h, None if el is None else el.ctypes.data, 0 if el is None else int(el.size), int(form), f(x),
+            f(ymf), f(nuf), f(phif), f(cohf), f(psif), float(dt), int(nl_isconv), int(last), evpt, stress, bodyload,
+            None if vmeps is None else vmeps.ctypes.data, None if scf is None else scf.ctypes.data)
+
     def set_control(self, cg_tol, cg_maxiter, nl_tol, nl_maxiter, phinu=0, allelastic=0):
         lib().orc_set_control(self.h, cg_tol, cg_maxiter, nl_tol, nl_maxiter, phinu, allelastic)
 
@@ -225,6 +239,22 @@ def pcg_solver(neq, nelmt, k, u, f, dprecon, gdof_elmt, cg_maxiter, cg_tol):
                                np.ascontiguousarray(gdof_elmt, np.int32).reshape(-1), cg_maxiter, cg_tol,
                                C.byref(it))
     return err, it.value
+
+
+def strength_reduction(srf, coh, nu, phi, psi, phinu=0):
+    """src/plastic_library.f90:42-88: (istat, cohf, nuf, phif, psif)."""
+    f = lambda a: np.ascontiguousarray(a, np.float64)
+    n = len(coh)
+    cohf, nuf, phif, psif = (np.zeros(n) for _ in range(4))
+    ist = lib().orc_strength_reduction(float(srf), int(phinu), n, f(coh), f(nu), f(phi), f(psi), cohf, nuf, phif,
+                                       psif)
+    return ist, cohf, nuf, phif, psif
+
+
+def dt_viscoplas(nuf, phif, ym):
+    """src/plastic_library.f90:17-39."""
+    f = lambda a: np.ascontiguousarray(a, np.float64)
+    return lib().orc_dt_viscoplas(len(nuf), f(nuf), f(phif), f(ym))
 
 
 def principal_stress(stress_global):

@@ -1333,12 +1333,24 @@ void orc_ebe_apply(int neq, int nelmt, const double* k, const double* p, const i
 }
 
 // One stress/yield/flow/body-load pass (the extracted src/slope.F90:311-383 block).
-double orc_stress_update(void* hv, const double* x, const double* ymf, const double* nuf, const double* phif,
-                         const double* cohf, const double* psif, double dt, int nl_isconv, int finalize,
-                         double* evpt, double* stress_elmt, double* bodyload) {
+// One pass of the stress block over elist (1-based, nel; NULL: all elements)
+// in the slope form (form 0) or the excavation form (form 1: pore pressure
+// before the stored stress, vmeps/scf accumulated when finalising).
+double orc_stress_update(void* hv, const int* elist, int nel, int form, const double* x, const double* ymf,
+                         const double* nuf, const double* phif, const double* cohf, const double* psif, double dt,
+                         int nl_isconv, int finalize, double* evpt, double* stress_elmt, double* bodyload,
+                         double* vmeps, double* scf) {
   OrcModel* h = (OrcModel*)hv;
-  return stress_update(h->M, nullptr, h->M.nelmt, x, h->M.gdof_elmt.data(), ymf, nuf, phif, cohf, psif, dt,
-                       nl_isconv != 0, finalize != 0, evpt, stress_elmt, bodyload, nullptr, nullptr);
+  std::vector<int> el0;
+  if (elist) {
+    el0.resize(nel);
+    for (int i = 0; i < nel; ++i) el0[i] = elist[i] - 1;
+  } else {
+    nel = h->M.nelmt;
+  }
+  return stress_update(h->M, elist ? el0.data() : nullptr, nel, x, h->M.gdof_elmt.data(), ymf, nuf, phif, cohf,
+                       psif, dt, nl_isconv != 0, finalize != 0, evpt, stress_elmt, bodyload,
+                       form == 1 ? vmeps : nullptr, form == 1 ? scf : nullptr, form == 1);
 }
 
 void orc_elastic_stress(void* hv, const double* x, double* stress_elmt) {

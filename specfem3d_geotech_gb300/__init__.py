@@ -40,7 +40,7 @@ EXPORTED = (
     "sg_principal_stress", "sg_write_summary_header", "sg_write_summary_row", "sg_write_ensight_case", "sg_write_ensight_geo",
     "sg_write_ensight_var", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
-    "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc",
+    "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc", "sg_stress_bodyload",
     "sg_server_create", "sg_server_submit", "sg_server_wait", "sg_server_stats", "sg_server_destroy",
 )
 
@@ -107,6 +107,9 @@ def lib(path: Optional[str] = None):
     L.sg_pcg_solve.argtypes = [vp, i, i, i, vp, vp, vp, vp, vp, i, d, C.POINTER(C.c_int), C.c_char_p]
     L.sg_pcg_solve_noalloc.restype = i
     L.sg_pcg_solve_noalloc.argtypes = [i, i, i, vp, vp, vp, vp, vp, i, d, C.POINTER(C.c_int), C.c_char_p]
+    L.sg_stress_bodyload.restype = i
+    L.sg_stress_bodyload.argtypes = [vp, i, i, i, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, d, i, i, vp, i, vp, i, vp,
+                                     vp, vp, vp, vp, vp, C.POINTER(C.c_double), C.c_char_p]
     L.sg_model_from_hex8.restype = vp
     L.sg_model_from_hex8.argtypes = [vp, i, vp, vp, vp, i, vp, vp, i, vp, vp, vp, i, C.c_char_p]
     L.sg_model_from_deck.restype = vp
@@ -269,6 +272,46 @@ def pcg_solver(neq: int, nelmt: int, k: np.ndarray, u: np.ndarray, f: np.ndarray
     if err not in (SG_OK, SG_ERR_NOCONV):
         raise SgError(err, tag.value.decode().strip() or ctx.last_error)
     return it.value, err, tag.value.decode().rstrip()
+
+
+def stress_bodyload(neq: int, nelmt: int, nnode: int, g_coord, g_num, gdof_elmt, mat_id, ym_blk, nuf_blk, phif_blk,
+                    cohf_blk, psif_blk, dt: float, nl_isconv: bool, last: bool, x, evpt: np.ndarray,
+                    stress_elmt: np.ndarray, bodyload: np.ndarray, elmt_list=None, wpressure=None, form: int = 0,
+                    vmeps: Optional[np.ndarray] = None, scf: Optional[np.ndarray] = None,
+                    ctx: Optional[Context] = None) -> float:
+    """Drop-in for the stress / yield / flow / body-load block of the plastic
+    loops (src/slope.F90:311-383, src/excavation.F90:546-616), on the GPU.
+
+    Reference layout and 1-based ids: ``g_num`` (nelmt, 27) nodes 1..nnode,
+    ``gdof_elmt`` (nelmt, 81), ``mat_id`` 1..nmatblk, ``elmt_list`` 1-based
+    (None: all elements).  ``evpt`` and ``stress_elmt`` (nelmt*27*6),
+    ``bodyload`` (neq+1) and, in the excavation form (``form=1``) when
+    ``last``, ``vmeps``/``scf`` (nnode) are float64 arrays updated in place.
+    Returns fmax.
+    """
+    ctx = ctx or default_context()
+    for name, a in (("evpt", evpt), ("stress_elmt", stress_elmt), ("bodyload", bodyload), ("vmeps", vmeps),
+                    ("scf", scf)):
+        if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous):
+            raise ValueError(f"{name} must be a C-contiguous float64 array")
+    f = lambda a: np.ascontiguousarray(a, np.float64)
+    i32 = lambda a: np.ascontiguousarray(a, np.int32)
+    gc, gn, ge, mi = f(g_coord), i32(g_num), i32(gdof_elmt), i32(mat_id)
+    props = [f(a) for a in (ym_blk, nuf_blk, phif_blk, cohf_blk, psif_blk)]
+    xv = f(x)
+    el = None if elmt_list is None else i32(elmt_list)
+    wp = None if wpressure is None else f(wpressure)
+    fm = C.c_double(0)
+    tag = C.create_string_buffer(ERRTAG_LEN + 1)
+    err = lib().sg_stress_bodyload(
+        ctx.h, neq, nelmt, nnode, _ptr(gc), _ptr(gn), _ptr(ge), _ptr(mi), len(props[0]), *(_ptr(a) for a in props),
+        float(dt), int(bool(nl_isconv)), int(bool(last)), None if el is None else _ptr(el),
+        0 if el is None else int(el.size), None if wp is None else _ptr(wp), int(form), _ptr(xv), _ptr(evpt),
+        _ptr(stress_elmt), _ptr(bodyload), None if vmeps is None else _ptr(vmeps), None if scf is None else _ptr(scf),
+        C.byref(fm), tag)
+    if err:
+        raise SgError(err, tag.value.decode().strip() or ctx.last_error)
+    return fm.value
 
 
 def pcg_solver_noalloc(neq: int, nelmt: int, k: np.ndarray, u: np.ndarray, f: np.ndarray, dprecon: np.ndarray,

@@ -13,6 +13,7 @@
 #include <array>
 #include <cstring>
 #include <functional>
+#include <numeric>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -75,6 +76,19 @@ struct sg_ctx {
     ColState* cs = nullptr;
     PcgGlobal* G = nullptr;
   } dropin;
+  // stress-block drop-in cache: mesh, dof map and element list of the last
+  // call (host copies for the content test) and their device forms
+  struct StressDropIn {
+    std::vector<double> coord;
+    std::vector<int> gnum, ge, mat, elist;
+    int nnode = -1, nelmt = -1, neq = -1, nel = -1;
+    GatherTopo T;  // groups of the listed elements' dof map
+    double *d_coord = nullptr, *d_geo = nullptr, *x = nullptr, *evpt = nullptr, *stress = nullptr, *bl = nullptr,
+           *Yb = nullptr, *wp = nullptr, *vm = nullptr, *sf = nullptr, *part = nullptr, *red = nullptr;
+    int *d_gnum = nullptr, *d_ge = nullptr, *d_mat = nullptr, *d_elist = nullptr;
+    MatF* mf = nullptr;
+    int mfcap = 0;
+  } sdrop;
 
   // CUDA graphs of PCG iteration chunks on small meshes, where launching
   // three short kernels per iteration from the host costs as much as running
@@ -1000,11 +1014,10 @@ static double dt_viscoplas(const std::vector<double>& nuf, const std::vector<dou
   return dtm;
 }
 
-static void make_matf(const HostMesh& h, const std::vector<double>& ymv, const std::vector<double>& nuf,
-                      const std::vector<double>& phif, const std::vector<double>& cohf,
-                      const std::vector<double>& psif, std::vector<MatF>& out) {
-  out.resize(h.nmatblk);
-  for (int i = 0; i < h.nmatblk; ++i) {
+static void make_matf(int nmat, const double* ymv, const double* nuf, const double* phif, const double* cohf,
+                      const double* psif, std::vector<MatF>& out) {
+  out.resize(nmat);
+  for (int i = 0; i < nmat; ++i) {
     double E = ymv[i], v = nuf[i];
     double Ef = E / ((1.0 + v) * (1.0 - 2.0 * v));
     MatF& m = out[i];
@@ -1180,7 +1193,7 @@ static int batch_add_impl(sg_model* M, double srf, int* slot_out) {
     B.restiff = true;
   }
   std::vector<MatF> mf;
-  make_matf(h, h.ym, nuf, phif, cohf, psif, mf);
+  make_matf(h.nmatblk, h.ym.data(), nuf.data(), phif.data(), cohf.data(), psif.data(), mf);
   cudaMemcpyAsync(W.mf + (size_t)j * h.nmatblk, mf.data(), sizeof(MatF) * h.nmatblk, cudaMemcpyHostToDevice, s);
   const int n1 = h.neq + 1;
   const size_t nst = (size_t)h.nelmt * NGLL * NST;
@@ -1492,7 +1505,7 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
   cudaMemsetAsync(stress, 0, sizeof(double) * nst, s);
   std::vector<double> cohf, nuf, phif, psif;
   std::vector<MatF> mf0;
-  make_matf(h, h.ym, h.nu, h.phi, h.coh, h.psi, mf0);
+  make_matf(h.nmatblk, h.ym.data(), h.nu.data(), h.phi.data(), h.coh.data(), h.psi.data(), mf0);
   MatF* d_mf = c->alloc<MatF>(nm);
   cudaMemcpyAsync(d_mf, mf0.data(), sizeof(MatF) * nm, cudaMemcpyHostToDevice, s);
   int status = SG_OK;
@@ -1599,7 +1612,7 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
         strength_reduction(h, srf, ctl->phinu != 0, cohf, nuf, phif, psif);
         double dt = dt_viscoplas(nuf, phif, h.ym, &ismat);
         std::vector<MatF> mf;
-        make_matf(h, h.ym, nuf, phif, cohf, psif, mf);
+        make_matf(h.nmatblk, h.ym.data(), nuf.data(), phif.data(), cohf.data(), psif.data(), mf);
         cudaMemcpyAsync(W.mf, mf.data(), sizeof(MatF) * nm, cudaMemcpyHostToDevice, s);
         double* d_nuf = c->alloc<double>(nm);
         cudaMemcpyAsync(d_nuf, nuf.data(), sizeof(double) * nm, cudaMemcpyHostToDevice, s);
@@ -1695,4 +1708,159 @@ done:
   c->release(d_mf);
   if (!c->check(cudaStreamSynchronize(s), "excavation") && status == SG_OK) status = SG_ERR_CUDA;
   return status;
+}
+
+// ---------------------------------------------------------------------------
+// The plastic iteration's stress / yield / flow / body-load block as a host
+// drop-in (src/slope.F90:311-383; excavation copy src/excavation.F90:546-616),
+// for a host that keeps its own plastic loop around sg_pcg_solve.  The mesh,
+// dof map, material ids and element list are uploaded (geometry computed, the
+// gather topology of the listed elements built) only when they differ from the
+// last call's; the plastic state goes in and out on every call.
+// ---------------------------------------------------------------------------
+static void release_sdrop(sg_ctx* c) {
+  auto& D = c->sdrop;
+  free_topo(c, D.T);
+  for (void* p : {(void*)D.d_coord, (void*)D.d_geo, (void*)D.x, (void*)D.evpt, (void*)D.stress, (void*)D.bl,
+                  (void*)D.Yb, (void*)D.wp, (void*)D.vm, (void*)D.sf, (void*)D.part, (void*)D.red, (void*)D.d_gnum,
+                  (void*)D.d_ge, (void*)D.d_mat, (void*)D.d_elist, (void*)D.mf})
+    c->release(p);
+  D = sg_ctx::StressDropIn();
+}
+
+extern "C" int sg_stress_bodyload(sg_ctx* c, int neq, int nelmt, int nnode, const double* g_coord, const int* g_num,
+                                  const int* gdof_elmt, const int* mat_id, int nmatblk, const double* ym_blk,
+                                  const double* nuf_blk, const double* phif_blk, const double* cohf_blk,
+                                  const double* psif_blk, double dt, int nl_isconv, int last, const int* elmt_list,
+                                  int nel, const double* wpressure, int form, const double* x, double* evpt,
+                                  double* stress_elmt, double* bodyload, double* vmeps, double* scf, double* fmax,
+                                  char* errtag) {
+  set_tag(errtag, "ERROR: unknown!");
+  if (!c) return SG_ERR_BADARG;
+  auto bad = [&](const char* m) { set_tag(errtag, m); return SG_ERR_BADARG; };
+  if (neq < 0 || nelmt < 0 || nnode <= 0 || nmatblk <= 0 || (form != 0 && form != 1) || !g_coord || !g_num ||
+      !gdof_elmt || !mat_id || !ym_blk || !nuf_blk || !phif_blk || !cohf_blk || !psif_blk || !x || !evpt ||
+      !stress_elmt || !bodyload || !fmax)
+    return bad("ERROR: bad argument to sg_stress_bodyload!");
+  if (!elmt_list) nel = nelmt;
+  if (nel < 0 || nel > nelmt) return bad("ERROR: element list longer than the mesh!");
+  for (size_t i = 0; i < (size_t)nelmt * NGLL; ++i)
+    if (g_num[i] < 1 || g_num[i] > nnode) return bad("ERROR: g_num entry out of [1,nnode]!");
+  for (size_t i = 0; i < (size_t)nelmt * NEDOF; ++i)
+    if (gdof_elmt[i] < 0 || gdof_elmt[i] > neq) return bad("ERROR: gdof_elmt entry out of [0,neq]!");
+  for (int e = 0; e < nelmt; ++e)
+    if (mat_id[e] < 1 || mat_id[e] > nmatblk) return bad("ERROR: mat_id entry out of [1,nmatblk]!");
+  if (elmt_list)
+    for (int i = 0; i < nel; ++i)
+      if (elmt_list[i] < 1 || elmt_list[i] > nelmt) return bad("ERROR: element list entry out of [1,nelmt]!");
+  cudaSetDevice(c->device);
+  cudaStream_t s = c->stream;
+  auto& D = c->sdrop;
+  const int n1 = neq + 1;
+  const size_t nst = (size_t)NST * NGLL * nelmt;
+  auto same = [](const auto& v, const auto* p, size_t n) {
+    return v.size() == n && (n == 0 || std::memcmp(v.data(), p, sizeof(*p) * n) == 0);
+  };
+  std::vector<int> el;
+  if (elmt_list) el.assign(elmt_list, elmt_list + nel);
+  else { el.resize(nel); std::iota(el.begin(), el.end(), 1); }
+  const bool hit = D.nnode == nnode && D.nelmt == nelmt && D.neq == neq && D.nel == nel &&
+                   same(D.coord, g_coord, (size_t)3 * nnode) && same(D.gnum, g_num, (size_t)NGLL * nelmt) &&
+                   same(D.ge, gdof_elmt, (size_t)NEDOF * nelmt) && same(D.mat, mat_id, (size_t)nelmt) &&
+                   D.elist == el;
+  if (!hit) {
+    release_sdrop(c);
+    D.coord.assign(g_coord, g_coord + (size_t)3 * nnode);
+    D.gnum.assign(g_num, g_num + (size_t)NGLL * nelmt);
+    D.ge.assign(gdof_elmt, gdof_elmt + (size_t)NEDOF * nelmt);
+    D.mat.assign(mat_id, mat_id + nelmt);
+    D.elist = el;
+    D.d_coord = c->alloc<double>((size_t)3 * nnode);
+    D.d_geo = c->alloc<double>((size_t)nelmt * NGLL * GEO_STRIDE);
+    D.x = c->alloc<double>(n1); D.bl = c->alloc<double>(n1);
+    D.evpt = c->alloc<double>(nst); D.stress = c->alloc<double>(nst);
+    D.Yb = c->alloc<double>((size_t)nel * NEDOF);
+    D.wp = c->alloc<double>(nnode);
+    D.vm = c->alloc<double>((size_t)nel * NGLL); D.sf = c->alloc<double>((size_t)nel * NGLL);
+    D.part = c->alloc<double>(NPART); D.red = c->alloc<double>(64);
+    D.d_gnum = c->alloc<int>((size_t)NGLL * nelmt); D.d_ge = c->alloc<int>((size_t)NEDOF * nelmt);
+    D.d_mat = c->alloc<int>(nelmt); D.d_elist = c->alloc<int>(nel);
+    // the topology of the listed elements' dof map, element slots in list order
+    std::vector<int> ge_sub((size_t)nel * NEDOF), gnum0((size_t)NGLL * nelmt), el0(nel);
+    for (int i = 0; i < nel; ++i) {
+      el0[i] = el[i] - 1;
+      std::memcpy(&ge_sub[(size_t)i * NEDOF], gdof_elmt + (size_t)el0[i] * NEDOF, sizeof(int) * NEDOF);
+    }
+    for (size_t i = 0; i < gnum0.size(); ++i) gnum0[i] = g_num[i] - 1;
+    build_groups_from_gdof(ge_sub.data(), nel, neq, D.T);
+    bool ok = D.d_coord && D.d_geo && D.x && D.bl && D.evpt && D.stress && D.Yb && D.wp && D.vm && D.sf && D.part &&
+              D.red && D.d_gnum && D.d_ge && D.d_mat && D.d_elist && upload_topo(c, D.T);
+    if (!ok) {
+      release_sdrop(c);
+      set_tag(errtag, "ERROR: out of device memory!");
+      return SG_ERR_OOM;
+    }
+    D.nnode = nnode; D.nelmt = nelmt; D.neq = neq; D.nel = nel;
+    cudaMemcpyAsync(D.d_coord, g_coord, sizeof(double) * 3 * nnode, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(D.d_gnum, gnum0.data(), sizeof(int) * gnum0.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(D.d_ge, gdof_elmt, sizeof(int) * (size_t)NEDOF * nelmt, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(D.d_mat, mat_id, sizeof(int) * nelmt, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(D.d_elist, el0.data(), sizeof(int) * nel, cudaMemcpyHostToDevice, s);
+    launch_geometry(D.d_coord, D.d_gnum, nelmt, D.d_geo, s);
+    // host copies above are read by the async copies: finish them before the vectors go
+    if (!c->check(cudaStreamSynchronize(s), "sg_stress_bodyload setup")) {
+      release_sdrop(c);
+      set_tag(errtag, "ERROR: CUDA failure: " + c->err);
+      return SG_ERR_CUDA;
+    }
+  }
+  if (D.mfcap < nmatblk) {
+    c->release(D.mf);
+    D.mf = c->alloc<MatF>(nmatblk);
+    D.mfcap = D.mf ? nmatblk : 0;
+    if (!D.mf) { set_tag(errtag, "ERROR: out of device memory!"); return SG_ERR_OOM; }
+  }
+  std::vector<MatF> mf;
+  make_matf(nmatblk, ym_blk, nuf_blk, phif_blk, cohf_blk, psif_blk, mf);
+  cudaMemcpyAsync(D.mf, mf.data(), sizeof(MatF) * nmatblk, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(D.x, x, sizeof(double) * n1, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(D.bl, bodyload, sizeof(double) * n1, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(D.evpt, evpt, sizeof(double) * nst, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(D.stress, stress_elmt, sizeof(double) * nst, cudaMemcpyHostToDevice, s);
+  if (wpressure) cudaMemcpyAsync(D.wp, wpressure, sizeof(double) * nnode, cudaMemcpyHostToDevice, s);
+  const bool fields = last && form == 1 && (vmeps || scf);
+  launch_stress_update(D.d_geo, D.d_elist, nel, D.d_ge, D.d_mat, D.x, 1, 0, D.mf, dt, nl_isconv, last, D.evpt,
+                       D.stress, D.Yb, 1, 0, D.part, D.T.d_pos, s, fields ? D.vm : nullptr, fields ? D.sf : nullptr,
+                       wpressure ? D.wp : nullptr, D.d_gnum, form);
+  double fm = 0.0;
+  reduce_read(c, D.part, NPART, 1, 1, 1, D.red, &fm);
+  // bodyload(egdof) += bload in element order, unless finalising; bodyload(0) = 0
+  if (!last) launch_gather_plain<double>(D.T, 1, D.Yb, D.bl, 1, nullptr, s);
+  cudaMemsetAsync(D.bl, 0, sizeof(double), s);
+  cudaMemcpyAsync(evpt, D.evpt, sizeof(double) * nst, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(stress_elmt, D.stress, sizeof(double) * nst, cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(bodyload, D.bl, sizeof(double) * n1, cudaMemcpyDeviceToHost, s);
+  std::vector<double> hv, hs;
+  if (fields) {
+    hv.resize((size_t)nel * NGLL); hs.resize((size_t)nel * NGLL);
+    cudaMemcpyAsync(hv.data(), D.vm, sizeof(double) * hv.size(), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hs.data(), D.sf, sizeof(double) * hs.size(), cudaMemcpyDeviceToHost, s);
+  }
+  if (!c->check(cudaStreamSynchronize(s), "sg_stress_bodyload")) {
+    set_tag(errtag, "ERROR: CUDA failure: " + c->err);
+    return SG_ERR_CUDA;
+  }
+  if (fields) {
+    // vmeps(num(i)) += sqrt(2/3 evpt.evpt), scf(num(i)) = min(scf, sf), in
+    // element-list then GLL order (src/excavation.F90:597-609)
+    for (int i = 0; i < nel; ++i)
+      for (int a = 0; a < NGLL; ++a) {
+        const int nd = g_num[(size_t)(el[i] - 1) * NGLL + a] - 1;
+        if (vmeps) vmeps[nd] = vmeps[nd] + hv[(size_t)i * NGLL + a];
+        if (scf && hs[(size_t)i * NGLL + a] < scf[nd]) scf[nd] = hs[(size_t)i * NGLL + a];
+      }
+  }
+  *fmax = fm;
+  set_tag(errtag, "");
+  return SG_OK;
 }

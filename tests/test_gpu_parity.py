@@ -586,3 +586,129 @@ def test_water_excavation_matches_oracle(ctx, tmp_path):
     assert ro[1, 2] > 2                                  # the water changes the second stage
     assert np.array_equal(r[:, 2], ro[:, 2])
     assert np.allclose(r[:, 3:5], ro[:, 3:5], rtol=1e-8)
+
+
+def _stress_inputs(mesh, om, srf):
+    from oracle.pyoracle import dt_viscoplas, strength_reduction
+    gam, ym, nu, phi, coh, psi = (mesh.props[:, i] for i in range(6))
+    _, cohf, nuf, phif, psif = strength_reduction(srf, coh, nu, phi, psi)
+    dt = dt_viscoplas(nuf, phif, ym)
+    a = om.arrays()
+    km, dp, ext = om.stiffness_bodyload()
+    dpi = np.zeros_like(dp)
+    dpi[1:] = 1.0 / dp[1:]
+    x = np.zeros(om.neq + 1)
+    orc_pcg(om.neq, om.nelmt, km, x, ext, dpi, a["gdof_elmt"], 5000, 1e-8)
+    return dict(props=(ym, nuf, phif, cohf, psif), dt=dt, a=a, x=x, km=km, dpi=dpi, ext=ext)
+
+
+def _gpu_pass(om, I, x, conv, last, ev, st, bl, **kw):
+    a = I["a"]
+    return sg.stress_bodyload(om.neq, om.nelmt, om.nnode, a["g_coord"], a["g_num"] + 1, a["gdof_elmt"], a["mat_id"],
+                              *I["props"], I["dt"], conv, last, x, ev, st, bl, **kw)
+
+
+# One pass of the stress block from identical inputs.  Most points agree to
+# rounding (1e-13), but points in axisymmetric states sit on the Lode corner,
+# sin(3 theta) = -3 sqrt(3) J3 / (2 J2^1.5) = +-1, where theta = asin(s)/3 has an
+# infinite derivative: a rounding delta ~ 1e-16 in s moves theta by
+# sqrt(2 delta)/3 ~ 5e-9 and with it the point's flow direction.  That is the
+# reference algorithm's own sensitivity, so the bounds are sqrt(eps)-scale: max
+# norms 1e-7 of the field's maximum (observed 2.2e-9), L2 norms 1e-9 (observed
+# 1.5e-10).
+PASS_MAX_TOL = 1e-7
+PASS_L2_TOL = 1e-9
+
+
+def test_stress_dropin_matches_oracle_passes(ctx):
+    """sg_stress_bodyload against the oracle's pass of src/slope.F90:311-383 on
+    the same inputs: three plastic passes from the same state, then the
+    finalising pass that stores the stress; a repeated call (cached mesh) is
+    bitwise equal."""
+    mesh = meshgen.slope2d(srf=(1.0,))
+    om = OracleModel(mesh)
+    I = _stress_inputs(mesh, om, 1.3)
+    nst = om.nelmt * 27 * 6
+    ev, st, bl = np.zeros(nst), np.zeros(nst), np.zeros(om.neq + 1)
+    x = I["x"].copy()
+    for it in range(4):
+        last = it == 3
+        evg, stg, blg = ev.copy(), st.copy(), bl.copy()
+        fg = _gpu_pass(om, I, x, False, last, evg, stg, blg)
+        ev2, st2, bl2 = ev.copy(), st.copy(), bl.copy()
+        fg2 = _gpu_pass(om, I, x, False, last, ev2, st2, bl2)
+        assert fg2 == fg and np.array_equal(ev2, evg) and np.array_equal(st2, stg) and np.array_equal(bl2, blg)
+        fo = om.stress_update(x, *I["props"], I["dt"], 0, int(last), ev, st, bl)
+        print(f"pass {it}: fmax {abs(fg - fo) / fo:.2e} evpt max {np.abs(evg - ev).max() / np.abs(ev).max():.2e} "
+              f"l2 {rel(evg, ev):.2e} bodyload {rel(blg, bl):.2e}")
+        assert fo > 0 and abs(fg - fo) <= 1e-12 * fo
+        assert np.abs(evg - ev).max() <= PASS_MAX_TOL * np.abs(ev).max() and rel(evg, ev) <= PASS_L2_TOL
+        assert rel(blg, bl) <= PASS_L2_TOL and blg[0] == 0.0
+        if last:
+            assert np.abs(stg - st.reshape(-1)).max() <= PASS_MAX_TOL * np.abs(st).max()
+        else:
+            load = I["ext"] + bl
+            load[0] = 0.0
+            orc_pcg(om.neq, om.nelmt, I["km"], x, load, I["dpi"], I["a"]["gdof_elmt"], 5000, 1e-8)
+            x[0] = 0.0
+
+
+def test_host_loop_with_gpu_dropins_matches_oracle_trial(ctx):
+    """The reference's plastic loop on the host around the two GPU drop-ins
+    (sg_pcg_solve, sg_stress_bodyload) gives the oracle's trial."""
+    from dropin_loop import host_trial
+    mesh = meshgen.slope2d(srf=(1.0,))
+    om = OracleModel(mesh)
+    a = om.arrays()
+
+    def pcg(neq, nelmt, km, x, load, dpi, ge, maxit, tol):
+        it, err, _ = sg.pcg_solver(neq, nelmt, km, x, load, dpi, ge, maxit, tol, ctx=ctx)
+        return err, it
+
+    def stress_pass(x, ym, nuf, phif, cohf, psif, dt, conv, last, ev, st, bl):
+        return sg.stress_bodyload(om.neq, om.nelmt, om.nnode, a["g_coord"], a["g_num"] + 1, a["gdof_elmt"],
+                                  a["mat_id"], ym, nuf, phif, cohf, psif, dt, conv, last, x, ev, st, bl, ctx=ctx)
+
+    r = host_trial(om, mesh, 1.0, pcg, stress_pass)
+    ro = om.trial(1.0, want_x=True, want_stress=True)
+    assert r["nl_iter"] == ro["nl_iter"] and r["converged"] == 1
+    assert rel(r["x"], ro["x"]) <= TRIAL_TOL
+    assert np.abs(r["stress"] - ro["stress"].reshape(-1)).max() <= STRESS_TOL * np.abs(ro["stress"]).max()
+    assert abs(r["fmax"] - ro["fmax"]) <= FMAX_TOL * abs(ro["fmax"])
+
+
+def test_stress_dropin_excavation_form(ctx, tmp_path):
+    """The excavation form over an element list (elmt_intact), with a water
+    table: pressure before the stored stress, vmeps/scf accumulated in list
+    order when finalising (src/excavation.F90:546-616)."""
+    mesh = meshgen.excavation(nx=6, ny=6, nz=4, L=12.0, H=8.0, pit=4.0, lifts=2, lift_h=2.0)
+    om = OracleModel(mesh)
+    om.set_water([1], _ws(tmp_path, "1\n0\n1 0.0 12.0 5.0\n"))
+    wp = om.pore_pressure()[0]
+    I = _stress_inputs(mesh, om, 1.0)
+    elist = np.flatnonzero(mesh.mat_id != 3) + 1            # the removed lifts' material stays out
+    assert 0 < elist.size < om.nelmt
+    nst = om.nelmt * 27 * 6
+    rng = np.random.default_rng(3)
+    st0 = -50.0 * rng.random(nst)                            # a stored (initial) stress
+    x = 3.0 * I["x"]
+    for last in (False, True):
+        ev, st, bl = np.zeros(nst), st0.copy(), np.zeros(om.neq + 1)
+        vm, sf = np.zeros(om.nnode), np.full(om.nnode, 1e32)
+        fo = om.stress_update(x, *I["props"], I["dt"], 0, int(last), ev, st, bl, elist=elist, form=1, vmeps=vm,
+                              scf=sf)
+        evg, stg, blg = np.zeros(nst), st0.copy(), np.zeros(om.neq + 1)
+        vmg, sfg = np.zeros(om.nnode), np.full(om.nnode, 1e32)
+        fg = _gpu_pass(om, I, x, False, last, evg, stg, blg, elmt_list=elist, wpressure=wp, form=1, vmeps=vmg,
+                       scf=sfg)
+        assert fo > 0 and abs(fg - fo) <= 1e-12 * fo
+        assert np.abs(evg - ev).max() <= PASS_MAX_TOL * np.abs(ev).max() and rel(evg, ev) <= PASS_L2_TOL
+        assert np.abs(stg - st).max() <= PASS_MAX_TOL * np.abs(st).max()
+        if last:
+            assert np.array_equal(blg, np.zeros_like(blg))
+            touched = sf < 1e32
+            assert np.array_equal(sfg < 1e32, touched) and (~touched).any()
+            np.testing.assert_allclose(sfg[touched], sf[touched], rtol=1e-9)
+            assert np.abs(vmg - vm).max() <= PASS_MAX_TOL * np.abs(vm).max()
+        else:
+            assert rel(blg, bl) <= PASS_L2_TOL
