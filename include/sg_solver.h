@@ -45,6 +45,7 @@ enum sg_precision {
 
 typedef struct sg_ctx sg_ctx;
 typedef struct sg_model sg_model;
+typedef struct sg_mesh sg_mesh;
 
 /* ---- context ---------------------------------------------------------- */
 /* Creates a context on CUDA device `device`.  hbm_budget = 0 means all free
@@ -117,6 +118,29 @@ int sg_stress_bodyload(sg_ctx* ctx, int neq, int nelmt, int nnode, const double*
 int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double* k, double* u, const double* f,
                          const double* dprecon, const int* gdof_elmt, int cg_maxiter, double cg_tol,
                          int* cg_iter, char* errtag);
+
+/* ---- host-only mesh (no device) ---------------------------------------- */
+/* Reads a .sem deck -- or a .psem deck, whose nproc, part_path and gfile
+ * entries are ignored and whose unpartitioned input files are read -- and
+ * builds the 27-node mesh, face constraints and node-major dof numbering on the
+ * host: read_input (src/read_input.f90:13-619), hex2spec (src/mesh_spec.f90:17-386)
+ * and apply_bc (src/apply_bc.f90:7-143), the same code sg_model_from_deck runs
+ * before it uploads.  Needs no GPU.  NULL with errtag (the reference's message
+ * where it has one) on failure. */
+sg_mesh* sg_mesh_from_deck(const char* sem_path, char* errtag);
+void sg_mesh_free(sg_mesh* mesh);
+/* info[0..7] = nnode, nelmt, neq, nmatblk, nsrf, nexcav, iswater, nwmat */
+int sg_mesh_info(const sg_mesh* mesh, int* info);
+/* g_coord[3*nnode], g_num[27*nelmt] (0-based), gdof[3*nnode], gdof_elmt[81*nelmt],
+ * mat_id[nelmt] (1-based), props[6*nmatblk] (gamma E nu phi c psi); any may be NULL. */
+int sg_mesh_arrays(const sg_mesh* mesh, double* g_coord, int* g_num, int* gdof, int* gdof_elmt, int* mat_id,
+                   double* props);
+/* dctl[8] = cg_tol, nl_tol, z0, s0, k0, eqkx, eqky, eqkz;
+ * ictl[8] = cg_maxiter, nl_maxiter, phinu, allelastic, nexcav, ninc, s0_type (-1: no
+ * stress0 line), iseqload; srf[nsrf]; nexcavid[nexcav] and excavid[sum of nexcavid];
+ * water_ids[nwmat]; any may be NULL. */
+int sg_mesh_control(const sg_mesh* mesh, double* dctl, int* ictl, double* srf, int* nexcavid, int* excavid,
+                    int* water_ids);
 
 /* ---- device-resident model -------------------------------------------- */
 /* Builds a spectral (27-node) model from an 8-node hex mesh: hex2spec with

@@ -40,7 +40,8 @@ EXPORTED = (
     "sg_principal_stress", "sg_write_summary_header", "sg_write_summary_row", "sg_write_ensight_case", "sg_write_ensight_geo",
     "sg_write_ensight_var", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
-    "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc", "sg_stress_bodyload",
+    "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc", "sg_stress_bodyload", "sg_mesh_from_deck", "sg_mesh_free", "sg_mesh_info",
+    "sg_mesh_arrays", "sg_mesh_control",
     "sg_server_create", "sg_server_submit", "sg_server_wait", "sg_server_stats", "sg_server_destroy",
 )
 
@@ -107,6 +108,15 @@ def lib(path: Optional[str] = None):
     L.sg_pcg_solve.argtypes = [vp, i, i, i, vp, vp, vp, vp, vp, i, d, C.POINTER(C.c_int), C.c_char_p]
     L.sg_pcg_solve_noalloc.restype = i
     L.sg_pcg_solve_noalloc.argtypes = [i, i, i, vp, vp, vp, vp, vp, i, d, C.POINTER(C.c_int), C.c_char_p]
+    L.sg_mesh_from_deck.restype = vp
+    L.sg_mesh_from_deck.argtypes = [C.c_char_p, C.c_char_p]
+    L.sg_mesh_free.argtypes = [vp]
+    L.sg_mesh_info.restype = i
+    L.sg_mesh_info.argtypes = [vp, vp]
+    L.sg_mesh_arrays.restype = i
+    L.sg_mesh_arrays.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.sg_mesh_control.restype = i
+    L.sg_mesh_control.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.sg_stress_bodyload.restype = i
     L.sg_stress_bodyload.argtypes = [vp, i, i, i, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, d, i, i, vp, i, vp, i, vp,
                                      vp, vp, vp, vp, vp, C.POINTER(C.c_double), C.c_char_p]
@@ -312,6 +322,44 @@ def stress_bodyload(neq: int, nelmt: int, nnode: int, g_coord, g_num, gdof_elmt,
     if err:
         raise SgError(err, tag.value.decode().strip() or ctx.last_error)
     return fm.value
+
+
+def read_deck(path: str) -> dict:
+    """Read a .sem / .psem deck and build the spectral mesh on the host (no GPU).
+
+    Returns the reference's arrays -- ``g_coord`` (nnode, 3), ``g_num``
+    (nelmt, 27) 0-based, ``gdof`` (nnode, 3), ``gdof_elmt`` (nelmt, 81),
+    ``mat_id`` (1-based), ``props`` (nmatblk, 6) -- and the control values;
+    raises :class:`SgError` with the reader's errtag on a bad deck.
+    """
+    L = lib()
+    tag = C.create_string_buffer(ERRTAG_LEN + 1)
+    h = L.sg_mesh_from_deck(str(path).encode(), tag)
+    if not h:
+        raise SgError(SG_ERR_BADARG, tag.value.decode().strip())
+    try:
+        info = np.zeros(8, np.int32)
+        L.sg_mesh_info(h, _ptr(info))
+        nnode, nelmt, neq, nmat, nsrf, nexcav, iswater, nwmat = (int(v) for v in info)
+        out = dict(nnode=nnode, nelmt=nelmt, neq=neq, nmatblk=nmat, iswater=iswater,
+                   g_coord=np.zeros((nnode, 3)), g_num=np.zeros((nelmt, 27), np.int32),
+                   gdof=np.zeros((nnode, 3), np.int32), gdof_elmt=np.zeros((nelmt, 81), np.int32),
+                   mat_id=np.zeros(nelmt, np.int32), props=np.zeros((nmat, 6)))
+        L.sg_mesh_arrays(h, *(_ptr(out[k]) for k in ("g_coord", "g_num", "gdof", "gdof_elmt", "mat_id", "props")))
+        dctl, ictl, srf = np.zeros(8), np.zeros(8, np.int32), np.zeros(max(nsrf, 1))
+        nexid = np.zeros(max(nexcav, 1), np.int32)
+        wids = np.zeros(max(nwmat, 1), np.int32)
+        L.sg_mesh_control(h, _ptr(dctl), _ptr(ictl), _ptr(srf), _ptr(nexid), None, _ptr(wids))
+        exid = np.zeros(max(int(nexid[:nexcav].sum()), 1), np.int32)
+        L.sg_mesh_control(h, None, None, None, None, _ptr(exid), None)
+        out.update(cg_tol=dctl[0], nl_tol=dctl[1], z0=dctl[2], s0=dctl[3], k0=dctl[4], eqk=tuple(dctl[5:8]),
+                   cg_maxiter=int(ictl[0]), nl_maxiter=int(ictl[1]), phinu=int(ictl[2]), allelastic=int(ictl[3]),
+                   nexcav=int(ictl[4]), ninc=int(ictl[5]), s0_type=int(ictl[6]), iseqload=int(ictl[7]),
+                   srf=srf[:nsrf].copy(), nexcavid=nexid[:nexcav].copy(),
+                   excavid=exid[:int(nexid[:nexcav].sum())].copy(), water_ids=wids[:nwmat].copy())
+        return out
+    finally:
+        L.sg_mesh_free(h)
 
 
 def pcg_solver_noalloc(neq: int, nelmt: int, k: np.ndarray, u: np.ndarray, f: np.ndarray, dprecon: np.ndarray,

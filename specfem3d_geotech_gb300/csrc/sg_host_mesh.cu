@@ -467,3 +467,98 @@ bool read_wsfile(const std::string& path, int nelmt, std::vector<WaterSurface>& 
 }
 
 }  // namespace sg
+
+// ---------------------------------------------------------------------------
+// Host-only mesh handle: the deck reader and mesh builder of
+// sg_model_from_deck without any device work (read_input, hex2spec and
+// apply_bc: src/read_input.f90:13-619, src/mesh_spec.f90:17-386,
+// src/apply_bc.f90:7-143).
+// ---------------------------------------------------------------------------
+struct sg_mesh {
+  sg::HostMesh H;
+  std::vector<double> props;  // nmatblk x [gamma E nu phi c psi]
+};
+
+namespace {
+void mesh_tag(char* errtag, const std::string& m) {
+  if (!errtag) return;
+  std::memset(errtag, ' ', SG_ERRTAG_LEN);
+  std::memcpy(errtag, m.data(), std::min<size_t>(m.size(), SG_ERRTAG_LEN));
+}
+}  // namespace
+
+extern "C" {
+
+sg_mesh* sg_mesh_from_deck(const char* path, char* errtag) {
+  mesh_tag(errtag, "ERROR: unknown!");
+  if (!path) return nullptr;
+  sg_mesh* m = new sg_mesh();
+  sg::HostMesh& H = m->H;
+  std::vector<double> x8, y8, z8;
+  std::vector<int> conn, mid, cnt, pairs;
+  std::string err;
+  if (!sg::read_deck(path, H, x8, y8, z8, conn, mid, m->props, cnt, pairs, err)) {
+    mesh_tag(errtag, err);
+    delete m;
+    return nullptr;
+  }
+  H.mat_id = mid;
+  for (int i = 0; i < H.nmatblk; ++i) {
+    const double* p = &m->props[(size_t)6 * i];
+    H.gam.push_back(p[0]); H.ym.push_back(p[1]); H.nu.push_back(p[2]);
+    H.phi.push_back(p[3]); H.coh.push_back(p[4]); H.psi.push_back(p[5]);
+  }
+  if (!sg::hex2spec(H, (int)x8.size(), x8.data(), y8.data(), z8.data(), conn.data(), err) ||
+      !sg::apply_bc(H, cnt.data(), pairs.data(), err)) {
+    mesh_tag(errtag, err);
+    delete m;
+    return nullptr;
+  }
+  sg::build_gdof_elmt(H);
+  mesh_tag(errtag, "");
+  return m;
+}
+
+void sg_mesh_free(sg_mesh* m) { delete m; }
+
+int sg_mesh_info(const sg_mesh* m, int* info) {
+  if (!m || !info) return SG_ERR_BADARG;
+  const sg::HostMesh& h = m->H;
+  info[0] = h.nnode; info[1] = h.nelmt; info[2] = h.neq; info[3] = h.nmatblk;
+  info[4] = (int)h.srf.size(); info[5] = h.nexcav; info[6] = h.iswater; info[7] = (int)h.water_ids.size();
+  return SG_OK;
+}
+
+int sg_mesh_arrays(const sg_mesh* m, double* g_coord, int* g_num, int* gdof, int* gdof_elmt, int* mat_id,
+                   double* props) {
+  if (!m) return SG_ERR_BADARG;
+  const sg::HostMesh& h = m->H;
+  if (g_coord) std::memcpy(g_coord, h.g_coord.data(), sizeof(double) * h.g_coord.size());
+  if (g_num) std::memcpy(g_num, h.g_num.data(), sizeof(int) * h.g_num.size());
+  if (gdof) std::memcpy(gdof, h.gdof.data(), sizeof(int) * h.gdof.size());
+  if (gdof_elmt) std::memcpy(gdof_elmt, h.gdof_elmt.data(), sizeof(int) * h.gdof_elmt.size());
+  if (mat_id) std::memcpy(mat_id, h.mat_id.data(), sizeof(int) * h.mat_id.size());
+  if (props) std::memcpy(props, m->props.data(), sizeof(double) * m->props.size());
+  return SG_OK;
+}
+
+int sg_mesh_control(const sg_mesh* m, double* dctl, int* ictl, double* srf, int* nexcavid, int* excavid,
+                    int* water_ids) {
+  if (!m) return SG_ERR_BADARG;
+  const sg::HostMesh& h = m->H;
+  if (dctl) {
+    const double v[8] = {h.cg_tol, h.nl_tol, h.z0, h.s0, h.k0, h.eqkx, h.eqky, h.eqkz};
+    std::memcpy(dctl, v, sizeof(v));
+  }
+  if (ictl) {
+    const int v[8] = {h.cg_maxiter, h.nl_maxiter, h.phinu, h.allelastic, h.nexcav, h.ninc, h.s0_type, h.iseqload};
+    std::memcpy(ictl, v, sizeof(v));
+  }
+  if (srf) std::memcpy(srf, h.srf.data(), sizeof(double) * h.srf.size());
+  if (nexcavid) std::memcpy(nexcavid, h.nexcavid.data(), sizeof(int) * h.nexcavid.size());
+  if (excavid) std::memcpy(excavid, h.excavid.data(), sizeof(int) * h.excavid.size());
+  if (water_ids) std::memcpy(water_ids, h.water_ids.data(), sizeof(int) * h.water_ids.size());
+  return SG_OK;
+}
+
+}  // extern "C"

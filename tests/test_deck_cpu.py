@@ -1,0 +1,88 @@
+"""The product's host deck reader and mesh builder (sg_mesh_from_deck: the
+code sg_model_from_deck runs before it uploads) against the oracle's, on CPU.
+
+Node numbering (get_global's merge), face constraints and node-major dof
+numbering are integer work and must be identical; coordinates are copied,
+so bitwise too.  Control values, the SRF list, the excavation lists, the
+stress0 and eqload lines and the water IDs are read as the reference reads
+them (src/read_input.f90:13-619); bad decks fail with its messages.
+"""
+import numpy as np
+import pytest
+
+import specfem3d_geotech_gb300 as sg
+from oracle.pyoracle import OracleModel
+from specfem3d_geotech_gb300 import meshgen
+
+
+def _same_mesh(r, om):
+    a = om.arrays()
+    assert (r["nnode"], r["nelmt"], r["neq"]) == (om.nnode, om.nelmt, om.neq)
+    for k in ("g_coord", "g_num", "gdof", "gdof_elmt", "mat_id"):
+        assert np.array_equal(r[k], a[k]), k
+    c = om.control()
+    for k in ("cg_tol", "nl_tol", "cg_maxiter", "nl_maxiter", "phinu", "allelastic"):
+        assert r[k] == c[k], k
+    assert np.array_equal(r["srf"], c["srf"])
+
+
+@pytest.mark.parametrize("name", ["slope2d", "slope3d", "excavation", "box"])
+def test_deck_matches_oracle(tmp_path, name):
+    mesh = {
+        "slope2d": lambda: meshgen.slope2d(),
+        "slope3d": lambda: meshgen.slope3d(nx=6, ny=3, nz=3),
+        "excavation": lambda: meshgen.excavation(nx=6, ny=6, nz=4, L=12.0, H=8.0, pit=4.0, lifts=2, lift_h=2.0),
+        "box": lambda: meshgen.box(nx=3, ny=2, nz=2),
+    }[name]()
+    deck = meshgen.write_deck(mesh, str(tmp_path))
+    r = sg.read_deck(deck)
+    _same_mesh(r, OracleModel(deck=deck))
+    assert np.array_equal(r["props"], mesh.props)
+    c = mesh.control
+    assert r["nexcav"] == c.nexcav and np.array_equal(r["excavid"], np.array(c.excavid, np.int32))
+    if c.nexcav:
+        assert np.array_equal(r["nexcavid"], np.ones(c.nexcav, np.int32)) and r["ninc"] == c.ninc
+    if mesh.stress0 is not None:
+        t, z0, s0, k0 = mesh.stress0
+        assert (r["s0_type"], r["z0"], r["s0"], r["k0"]) == (t, z0, s0, k0)
+    else:
+        assert r["s0_type"] == -1
+
+
+def test_optional_lines(tmp_path):
+    """eqload: and water: lines and the material list's water IDs."""
+    mesh = meshgen.slope2d(srf=(1.0, 1.2))
+    mesh.water = ((1,), "1\n0\n1 0.0 20.0 4.0\n")
+    deck = meshgen.write_deck(mesh, str(tmp_path))
+    with open(deck, "a") as f:
+        f.write("eqload: eqkx=0.1, eqky=0.0, eqkz=-0.05\n")
+    r = sg.read_deck(deck)
+    assert r["iswater"] == 1 and np.array_equal(r["water_ids"], [1])
+    assert r["iseqload"] == 1 and r["eqk"] == (0.1, 0.0, -0.05)
+    assert np.array_equal(r["srf"], [1.0, 1.2])
+    _same_mesh(r, OracleModel(deck=deck))
+
+
+def _err(path):
+    with pytest.raises(sg.SgError) as e:
+        sg.read_deck(path)
+    return str(e.value)
+
+
+def test_bad_decks(tmp_path):
+    mesh = meshgen.slope2d(srf=(1.0,))
+    deck = meshgen.write_deck(mesh, str(tmp_path))
+    text = open(deck).read()
+    assert "cannot be opened" in _err(str(tmp_path / "missing.sem"))
+    bad = tmp_path / "dup.sem"
+    bad.write_text(text + "eqload: eqkx=0.1\neqload: eqkx=0.2\n")
+    assert "copy of line type eqload: not permitted" in _err(str(bad))
+    bad = tmp_path / "token.sem"
+    bad.write_text(text + "gravity: g=9.81\n")
+    assert 'invalid line type: "gravity:"' in _err(str(bad))
+    bad = tmp_path / "water.sem"
+    bad.write_text(text + "water: wsfile='ws'\n")     # no water IDs after the material blocks
+    assert "water IDs cannot be read from material list" in _err(str(bad))
+    bad = tmp_path / "nocontrol.sem"
+    bad.write_text("\n".join(l for l in text.splitlines() if not l.startswith("control:")) + "\n")
+    assert 'cannot read the "control:" line' in _err(str(bad))
