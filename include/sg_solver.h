@@ -284,13 +284,13 @@ int sg_srf_sweep(sg_model* model, const sg_control* ctl, int nsrf, const double*
 int sg_fos(sg_model* model, const sg_control* ctl, double lo, double hi, double step, int k,
            double* fos, int* ntrials, int* nrounds);
 
-/* ---- request loop: factor-of-safety solves of many meshes ---------------
+/* ---- request loop: factor-of-safety and excavation solves of many meshes --
  * Requests are queued on submission and admitted in arrival order when their
  * estimated HBM footprint fits the server's budget (hbm_budget = 0: 90 % of
  * free device memory).  `workers` threads each own a context and stream, so
- * admitted requests run concurrently on the device; inside a request the SRF
- * search is sg_fos with k batched trials.  Times are seconds since the server
- * was created. */
+ * admitted requests run concurrently on the device; inside a factor-of-safety
+ * request the SRF search is sg_fos with k batched trials, an excavation
+ * request runs sg_excavation.  Times are seconds since the server was created. */
 typedef struct sg_server sg_server;
 typedef struct sg_fos_result {
   int id, status;
@@ -298,12 +298,24 @@ typedef struct sg_fos_result {
   int ntrials, nrounds, nelmt, neq;
   double footprint, hbm_bytes;        /* admission estimate, device bytes used */
   double t_arrival, t_start, t_done;
+  int kind;    /* 0 factor of safety; 1 staged excavation (fos unused, ntrials = plastic
+                  iterations over the stages run, rows from sg_server_stages) */
+  int nstage;  /* excavation: stages run */
 } sg_fos_result;
 sg_server* sg_server_create(int device, size_t hbm_budget, int workers);
 int sg_server_submit(sg_server* server, int nnode8, const double* x8, const double* y8, const double* z8,
                      int nelmt, const int* conn8, const int* mat_id, int nmatblk, const double* props,
                      const int* bc_counts, const int* bc_pairs, const sg_control* ctl, double lo,
                      double hi, double step, int k, int* id);
+/* Queues a staged-excavation request (sg_excavation on its own model; the
+ * stage arguments as there), admitted by its footprint like the others. */
+int sg_server_submit_excavation(sg_server* server, int nnode8, const double* x8, const double* y8,
+                                const double* z8, int nelmt, const int* conn8, const int* mat_id, int nmatblk,
+                                const double* props, const int* bc_counts, const int* bc_pairs,
+                                const sg_control* ctl, int s0_type, double z0, double s0, double k0, int nexcav,
+                                const int* nexcavid, const int* excavid, int ninc, double srf, int* id);
+/* The stage rows of a finished excavation request (nstage rows of 8, as sg_excavation). */
+int sg_server_stages(sg_server* server, int id, double* stage_res);
 /* Blocks until request `id` is done (or timeout_s passes: SG_ERR_TIMEOUT). */
 int sg_server_wait(sg_server* server, int id, double timeout_s, sg_fos_result* result);
 /* stats[0..5] = completed, p50 latency, p99 latency (arrival to done, s),

@@ -42,7 +42,7 @@ EXPORTED = (
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
     "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc", "sg_stress_bodyload", "sg_mesh_from_deck", "sg_mesh_free", "sg_mesh_info",
     "sg_mesh_arrays", "sg_mesh_control",
-    "sg_server_create", "sg_server_submit", "sg_server_wait", "sg_server_stats", "sg_server_destroy",
+    "sg_server_create", "sg_server_submit", "sg_server_submit_excavation", "sg_server_stages", "sg_server_wait", "sg_server_stats", "sg_server_destroy",
 )
 
 
@@ -66,7 +66,7 @@ class FosResult(C.Structure):
     _fields_ = [("id", C.c_int), ("status", C.c_int), ("fos", C.c_double), ("ntrials", C.c_int),
                 ("nrounds", C.c_int), ("nelmt", C.c_int), ("neq", C.c_int), ("footprint", C.c_double),
                 ("hbm_bytes", C.c_double), ("t_arrival", C.c_double), ("t_start", C.c_double),
-                ("t_done", C.c_double)]
+                ("t_done", C.c_double), ("kind", C.c_int), ("nstage", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -189,6 +189,11 @@ def lib(path: Optional[str] = None):
     L.sg_server_submit.restype = i
     L.sg_server_submit.argtypes = [vp, i, vp, vp, vp, i, vp, vp, i, vp, vp, vp, C.POINTER(Control), d, d, d, i,
                                    C.POINTER(C.c_int)]
+    L.sg_server_submit_excavation.restype = i
+    L.sg_server_submit_excavation.argtypes = [vp, i, vp, vp, vp, i, vp, vp, i, vp, vp, vp, C.POINTER(Control), i, d,
+                                              d, d, i, vp, vp, i, d, C.POINTER(C.c_int)]
+    L.sg_server_stages.restype = i
+    L.sg_server_stages.argtypes = [vp, i, vp]
     L.sg_server_wait.restype = i
     L.sg_server_wait.argtypes = [vp, i, d, C.POINTER(FosResult)]
     L.sg_server_stats.restype = i
@@ -610,13 +615,16 @@ class Server:
             raise SgError(SG_ERR_NODEVICE, "sg_server_create failed")
         self._keep = {}
 
-    def submit(self, mesh, ctl: Control, lo: float = 1.0, hi: float = 3.0, step: float = 0.01, k: int = 8) -> int:
-        arrs = [np.ascontiguousarray(mesh.x, np.float64), np.ascontiguousarray(mesh.y, np.float64),
+    @staticmethod
+    def _mesh_arrays(mesh):
+        return [np.ascontiguousarray(mesh.x, np.float64), np.ascontiguousarray(mesh.y, np.float64),
                 np.ascontiguousarray(mesh.z, np.float64), np.ascontiguousarray(mesh.conn.reshape(-1), np.int32),
                 np.ascontiguousarray(mesh.mat_id, np.int32), np.ascontiguousarray(mesh.props.reshape(-1), np.float64),
                 np.array([b.shape[0] for b in mesh.bc], np.int32),
                 np.ascontiguousarray(np.concatenate(mesh.bc).reshape(-1), np.int32)]
-        x, y, z, conn, mid, props, cnt, pairs = arrs
+
+    def submit(self, mesh, ctl: Control, lo: float = 1.0, hi: float = 3.0, step: float = 0.01, k: int = 8) -> int:
+        x, y, z, conn, mid, props, cnt, pairs = self._mesh_arrays(mesh)
         rid = C.c_int(0)
         st = lib().sg_server_submit(self.h, mesh.nnode8, _ptr(x), _ptr(y), _ptr(z), mesh.nelmt, _ptr(conn), _ptr(mid),
                                     mesh.props.shape[0], _ptr(props), _ptr(cnt), _ptr(pairs), C.byref(ctl), lo, hi,
@@ -625,12 +633,33 @@ class Server:
             raise SgError(st, "sg_server_submit")
         return rid.value
 
+    def submit_excavation(self, mesh, ctl: Control, s0_type: int, z0: float, s0: float, k0: float,
+                          excavid: Sequence[int], ninc: int = 1, srf: float = 1.0,
+                          nexcavid: Optional[Sequence[int]] = None) -> int:
+        """Queue a staged-excavation request (sg_excavation on its own model)."""
+        x, y, z, conn, mid, props, cnt, pairs = self._mesh_arrays(mesh)
+        exid = np.ascontiguousarray(excavid, np.int32)
+        nexid = np.ascontiguousarray(np.ones(exid.size) if nexcavid is None else nexcavid, np.int32)
+        rid = C.c_int(0)
+        st = lib().sg_server_submit_excavation(
+            self.h, mesh.nnode8, _ptr(x), _ptr(y), _ptr(z), mesh.nelmt, _ptr(conn), _ptr(mid), mesh.props.shape[0],
+            _ptr(props), _ptr(cnt), _ptr(pairs), C.byref(ctl), s0_type, z0, s0, k0, int(nexid.size), _ptr(nexid),
+            _ptr(exid), ninc, srf, C.byref(rid))
+        if st:
+            raise SgError(st, "sg_server_submit_excavation")
+        return rid.value
+
     def wait(self, rid: int, timeout: float = 3600.0):
         r = FosResult()
         st = lib().sg_server_wait(self.h, rid, timeout, C.byref(r))
         if st:
             raise SgError(st, "sg_server_wait")
-        return r.as_dict()
+        out = r.as_dict()
+        if r.kind == 1:
+            rows = np.zeros(8 * max(r.nstage, 1))
+            lib().sg_server_stages(self.h, rid, _ptr(rows))
+            out["stages"] = rows[:8 * r.nstage].reshape(-1, 8)
+        return out
 
     def stats(self):
         o = np.zeros(6)

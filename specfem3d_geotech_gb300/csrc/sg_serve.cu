@@ -1,8 +1,9 @@
-// sg_serve.cu -- device-resident request loop for factor-of-safety solves.
+// sg_serve.cu -- device-resident request loop for factor-of-safety and
+// staged-excavation solves.
 //
-// Requests (each its own hex8 mesh, control and SRF search) are queued on
-// submission and admitted in arrival order when their HBM footprint fits the
-// server's budget.  Each worker thread owns a context (its own CUDA stream),
+// Requests (each its own hex8 mesh and control, with an SRF search or a list
+// of excavation stages) are queued on submission and admitted in arrival
+// order when their HBM footprint fits the server's budget.  Each worker thread owns a context (its own CUDA stream),
 // so admitted requests run concurrently and their kernels overlap on the
 // device; inside a request the SRF trials run as a continuously refilled
 // batch (sg_fos: k probes per k-section round share every element apply).
@@ -32,6 +33,11 @@ struct Request {
   sg_control ctl{};
   double lo = 1.0, hi = 3.0, step = 0.01;
   int k = 1;
+  // kind 1: staged excavation (sg_excavation) instead of the SRF search
+  int kind = 0, s0_type = 1, nexcav = 0, ninc = 1;
+  double z0 = 0, s0 = 0, k0 = 0, srf = 1.0;
+  std::vector<int> nexcavid, excavid;
+  std::vector<double> stage_res;
   size_t footprint = 0;
   Clock::time_point t_arrival, t_start, t_done;
   int state = 0;  // 0 queued, 1 running, 2 done
@@ -50,6 +56,14 @@ size_t estimate_footprint(int nelmt, int k, int precision) {
     b += ne * sg::KS_STRIDE * 4 + ne * sg::NGLL * sg::MF_REC * 4 + ne * 81 * kr * 4 + neq * kr * 4 * 6;
   b += kr * ne * 27 * 6 * 8 * 2 + ne * 81 * kr * 8 + neq * kr * 8 * 8 + ne * 27 * 4 * 2;
   return b + (b >> 3) + (size_t(64) << 20);
+}
+
+// An excavation request: one trial's model and plastic state plus the stage
+// work arrays (the intact / void element lists and dof maps, the stage's
+// gather topologies and the per-point plastic-strain and safety-factor fields).
+size_t estimate_excavation_footprint(int nelmt, int precision) {
+  const size_t ne = (size_t)nelmt;
+  return estimate_footprint(nelmt, 1, precision) + ne * (81 * 4 * 2 + 27 * 8 * 2 + 27 * 4 * 4 + 16);
 }
 
 }  // namespace
@@ -104,7 +118,15 @@ static void worker_main(sg_server* S) {
         sg_model_info(m, info);
         res.nelmt = info[1];
         res.neq = info[2];
-        res.status = sg_fos(m, &r->ctl, r->lo, r->hi, r->step, r->k, &res.fos, &res.ntrials, &res.nrounds);
+        if (r->kind == 1) {
+          res.kind = 1;
+          r->stage_res.assign((size_t)8 * r->nexcav, 0.0);
+          res.status = sg_excavation(m, &r->ctl, r->s0_type, r->z0, r->s0, r->k0, r->nexcav, r->nexcavid.data(),
+                                     r->excavid.data(), r->ninc, r->srf, r->stage_res.data(), &res.nstage);
+          for (int st = 0; st < res.nstage; ++st) res.ntrials += (int)r->stage_res[(size_t)8 * st + 2];
+        } else {
+          res.status = sg_fos(m, &r->ctl, r->lo, r->hi, r->step, r->k, &res.fos, &res.ntrials, &res.nrounds);
+        }
         res.hbm_bytes = (double)sg_hbm_used(ctx);
         sg_model_free(m);
       }
@@ -150,13 +172,9 @@ sg_server* sg_server_create(int device, size_t hbm_budget, int workers) {
   return S;
 }
 
-int sg_server_submit(sg_server* S, int nnode8, const double* x8, const double* y8, const double* z8, int nelmt,
-                     const int* conn8, const int* mat_id, int nmatblk, const double* props, const int* bc_counts,
-                     const int* bc_pairs, const sg_control* ctl, double lo, double hi, double step, int k,
-                     int* id) {
-  if (!S || nnode8 <= 0 || nelmt <= 0 || nmatblk <= 0 || !x8 || !y8 || !z8 || !conn8 || !mat_id || !props ||
-      !bc_counts || !bc_pairs || !ctl || k < 1 || k > 16 || !(hi > lo) || !(step > 0))
-    return SG_ERR_BADARG;
+static Request* new_request(int nnode8, const double* x8, const double* y8, const double* z8, int nelmt,
+                            const int* conn8, const int* mat_id, int nmatblk, const double* props,
+                            const int* bc_counts, const int* bc_pairs, const sg_control* ctl) {
   Request* r = new Request();
   r->nnode8 = nnode8; r->nelmt = nelmt; r->nmatblk = nmatblk;
   r->x8.assign(x8, x8 + nnode8); r->y8.assign(y8, y8 + nnode8); r->z8.assign(z8, z8 + nnode8);
@@ -167,8 +185,10 @@ int sg_server_submit(sg_server* S, int nnode8, const double* x8, const double* y
   size_t npairs = (size_t)bc_counts[0] + bc_counts[1] + bc_counts[2];
   r->bc_pairs.assign(bc_pairs, bc_pairs + 2 * npairs);
   r->ctl = *ctl;
-  r->lo = lo; r->hi = hi; r->step = step; r->k = k;
-  r->footprint = estimate_footprint(nelmt, k, ctl->precision);
+  return r;
+}
+
+static int enqueue(sg_server* S, Request* r, int* id) {
   {
     std::lock_guard<std::mutex> lk(S->mu);
     if (r->footprint > S->budget) { delete r; return SG_ERR_OOM; }
@@ -176,9 +196,55 @@ int sg_server_submit(sg_server* S, int nnode8, const double* x8, const double* y
     r->t_arrival = Clock::now();
     S->all[r->id] = r;
     S->queue.push_back(r);
+    if (id) *id = r->id;
   }
   S->cv.notify_all();
-  if (id) *id = r->id;
+  return SG_OK;
+}
+
+int sg_server_submit(sg_server* S, int nnode8, const double* x8, const double* y8, const double* z8, int nelmt,
+                     const int* conn8, const int* mat_id, int nmatblk, const double* props, const int* bc_counts,
+                     const int* bc_pairs, const sg_control* ctl, double lo, double hi, double step, int k,
+                     int* id) {
+  if (!S || nnode8 <= 0 || nelmt <= 0 || nmatblk <= 0 || !x8 || !y8 || !z8 || !conn8 || !mat_id || !props ||
+      !bc_counts || !bc_pairs || !ctl || k < 1 || k > 16 || !(hi > lo) || !(step > 0))
+    return SG_ERR_BADARG;
+  Request* r = new_request(nnode8, x8, y8, z8, nelmt, conn8, mat_id, nmatblk, props, bc_counts, bc_pairs, ctl);
+  r->lo = lo; r->hi = hi; r->step = step; r->k = k;
+  r->footprint = estimate_footprint(nelmt, k, ctl->precision);
+  return enqueue(S, r, id);
+}
+
+int sg_server_submit_excavation(sg_server* S, int nnode8, const double* x8, const double* y8, const double* z8,
+                                int nelmt, const int* conn8, const int* mat_id, int nmatblk, const double* props,
+                                const int* bc_counts, const int* bc_pairs, const sg_control* ctl, int s0_type,
+                                double z0, double s0, double k0, int nexcav, const int* nexcavid,
+                                const int* excavid, int ninc, double srf, int* id) {
+  if (!S || nnode8 <= 0 || nelmt <= 0 || nmatblk <= 0 || !x8 || !y8 || !z8 || !conn8 || !mat_id || !props ||
+      !bc_counts || !bc_pairs || !ctl || nexcav < 1 || !nexcavid || !excavid || ninc < 1 || !(srf > 0))
+    return SG_ERR_BADARG;
+  size_t nid = 0;
+  for (int i = 0; i < nexcav; ++i) {
+    if (nexcavid[i] < 1) return SG_ERR_BADARG;
+    nid += (size_t)nexcavid[i];
+  }
+  Request* r = new_request(nnode8, x8, y8, z8, nelmt, conn8, mat_id, nmatblk, props, bc_counts, bc_pairs, ctl);
+  r->kind = 1;
+  r->s0_type = s0_type; r->z0 = z0; r->s0 = s0; r->k0 = k0;
+  r->nexcav = nexcav; r->ninc = ninc; r->srf = srf;
+  r->nexcavid.assign(nexcavid, nexcavid + nexcav);
+  r->excavid.assign(excavid, excavid + nid);
+  r->footprint = estimate_excavation_footprint(nelmt, ctl->precision);
+  return enqueue(S, r, id);
+}
+
+int sg_server_stages(sg_server* S, int id, double* stage_res) {
+  if (!S || !stage_res) return SG_ERR_BADARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  auto it = S->all.find(id);
+  if (it == S->all.end() || it->second->kind != 1 || it->second->state != 2) return SG_ERR_BADARG;
+  const Request* r = it->second;
+  std::memcpy(stage_res, r->stage_res.data(), sizeof(double) * (size_t)8 * r->res.nstage);
   return SG_OK;
 }
 

@@ -59,3 +59,29 @@ def test_admission_by_hbm_footprint(ctx):
     # arrival-order admission: each starts after the previous one finished
     for a, b in zip(got, got[1:]):
         assert b["t_start"] >= a["t_done"] - 1e-3
+
+
+def test_excavation_requests_in_the_mix(ctx):
+    """Staged-excavation requests admitted beside factor-of-safety requests
+    give the same stage results as the same excavation run alone, and the
+    mixed requests overlap on the device."""
+    exc = meshgen.excavation(nx=6, ny=6, nz=4, L=12.0, H=8.0, pit=4.0, lifts=2, lift_h=2.0)
+    ctl64 = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=200)
+    model = sg.Model(exc, ctx=ctx)
+    alone = model.excavation(ctl64, 1, 8.0, 0.0, 0.5, [2, 3])
+    model.close()
+    slopes = requests(2, seed=6)
+    ctl = control()
+    srv = sg.Server(0, 0, workers=3)
+    ids = [srv.submit(slopes[0], ctl, lo=1.0, hi=2.0, step=0.1, k=4),
+           srv.submit_excavation(exc, ctl64, 1, 8.0, 0.0, 0.5, [2, 3]),
+           srv.submit(slopes[1], ctl, lo=1.0, hi=2.0, step=0.1, k=4)]
+    got = [srv.wait(i, timeout=600) for i in ids]
+    st = srv.stats()
+    srv.close()
+    g = got[1]
+    assert g["status"] == 0 and g["kind"] == 1 and g["nstage"] == alone.shape[0]
+    assert np.array_equal(g["stages"], alone)          # same device code, same order: bitwise
+    assert g["ntrials"] == int(alone[:, 2].sum())
+    assert all(r["status"] == 0 and r["kind"] == 0 for r in (got[0], got[2]))
+    assert st["completed"] == 3 and st["peak_concurrent"] >= 2
