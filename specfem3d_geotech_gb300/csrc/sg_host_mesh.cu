@@ -10,6 +10,7 @@
 #include <map>
 #include <numeric>
 #include <sstream>
+#include <thread>
 
 #include "sg_internal.h"
 
@@ -33,6 +34,104 @@ bool on_face(int n, int face) {
   return false;
 }
 
+}  // namespace
+
+namespace {
+// Host threads for the mesh build (capped: the server may build several meshes at once).
+int host_threads() {
+  unsigned h = std::thread::hardware_concurrency();
+  return (int)std::max(1u, std::min(h, 16u));
+}
+
+template <typename F>
+void parallel_ranges(size_t n, int nt, F f) {
+  if (nt <= 1 || n < 65536) { f(size_t(0), n); return; }
+  std::vector<std::thread> th;
+  const size_t step = (n + nt - 1) / nt;
+  for (int t = 0; t < nt; ++t) {
+    const size_t a = t * step, b = std::min(n, a + step);
+    if (a >= b) break;
+    th.emplace_back(f, a, b);
+  }
+  for (auto& x : th) x.join();
+}
+
+struct KeyIdx {
+  double k;
+  int i;
+};
+
+// get_global's ordering (src/mesh_spec.f90:146-262): three passes, x then y
+// then z.  Each pass stable-sorts every current segment by that coordinate
+// and then starts a new segment wherever the coordinate jumps by more than tol
+// from its predecessor.  The first pass is one segment, sorted as stable-sorted
+// chunks joined by stable merges; the later passes sort their segments
+// independently.  Stability at every step keeps the order exactly that of one
+// sequential stable sort per segment.
+void merge_order(const std::vector<double>* keys[3], size_t np, double tol, std::vector<int>& order,
+                 std::vector<char>& seg) {
+  const int nt = host_threads();
+  order.resize(np);
+  std::iota(order.begin(), order.end(), 0);
+  seg.assign(np, 0);
+  if (np == 0) return;
+  seg[0] = 1;
+  auto less = [](const KeyIdx& p, const KeyIdx& q) { return p.k < q.k; };
+  std::vector<KeyIdx> buf(np), tmp;
+  for (int d = 0; d < 3; ++d) {
+    const std::vector<double>& key = *keys[d];
+    parallel_ranges(np, nt, [&](size_t a, size_t b) {
+      for (size_t i = a; i < b; ++i) buf[i] = {key[order[i]], order[i]};
+    });
+    if (d == 0) {
+      const int nc = (int)std::max<size_t>(1, std::min<size_t>((size_t)nt, np / 65536));
+      std::vector<size_t> cut(nc + 1);
+      for (int c = 0; c <= nc; ++c) cut[c] = np * c / nc;
+      {
+        std::vector<std::thread> th;
+        for (int c = 0; c < nc; ++c)
+          th.emplace_back([&, c] { std::stable_sort(buf.begin() + cut[c], buf.begin() + cut[c + 1], less); });
+        for (auto& x : th) x.join();
+      }
+      tmp.resize(np);
+      while (cut.size() > 2) {
+        std::vector<size_t> nx;
+        std::vector<std::thread> th;
+        size_t c = 0;
+        for (; c + 2 < cut.size(); c += 2) {
+          const size_t a = cut[c], m = cut[c + 1], b = cut[c + 2];
+          th.emplace_back([&, a, m, b] {
+            std::merge(buf.begin() + a, buf.begin() + m, buf.begin() + m, buf.begin() + b, tmp.begin() + a, less);
+          });
+          nx.push_back(a);
+        }
+        if (c + 1 < cut.size()) {  // an unpaired last chunk is carried over
+          std::copy(buf.begin() + cut[c], buf.begin() + cut[c + 1], tmp.begin() + cut[c]);
+          nx.push_back(cut[c]);
+        }
+        nx.push_back(np);
+        for (auto& x : th) x.join();
+        std::swap(buf, tmp);
+        cut.swap(nx);
+      }
+    } else {
+      std::vector<size_t> starts;
+      for (size_t i = 0; i < np; ++i)
+        if (seg[i]) starts.push_back(i);
+      starts.push_back(np);
+      const size_t ns = starts.size() - 1;
+      parallel_ranges(ns, nt, [&](size_t a, size_t b) {
+        for (size_t u = a; u < b; ++u)
+          if (starts[u + 1] - starts[u] > 1) std::stable_sort(buf.begin() + starts[u], buf.begin() + starts[u + 1], less);
+      });
+    }
+    parallel_ranges(np, nt, [&](size_t a, size_t b) {
+      for (size_t i = a; i < b; ++i) order[i] = buf[i].i;
+      for (size_t i = std::max<size_t>(a, 1); i < b; ++i)
+        if (std::fabs(buf[i].k - buf[i - 1].k) > tol) seg[i] = 1;
+    });
+  }
+}
 }  // namespace
 
 // hex2spec (src/mesh_spec.f90:17-143): GLL point coordinates from the
@@ -61,46 +160,33 @@ bool hex2spec(HostMesh& M, int nnode8, const double* x8, const double* y8, const
   double xmin = x8[0], xmax = x8[0];
   for (int i = 0; i < nnode8; ++i) { xmin = std::min(xmin, x8[i]); xmax = std::max(xmax, x8[i]); }
   const size_t np = (size_t)nelmt * NGLL;
+  for (size_t t = 0; t < (size_t)nelmt * 8; ++t)
+    if (conn8[t] < 1 || conn8[t] > nnode8) { err = "ERROR: connectivity references a node out of range!"; return false; }
   std::vector<double> xs(np), ys(np), zs(np);
-  for (int e = 0; e < nelmt; ++e) {
-    int c[8];
-    for (int g = 0; g < 8; ++g) {
-      c[g] = conn8[(size_t)e * 8 + g] - 1;
-      if (c[g] < 0 || c[g] >= nnode8) { err = "ERROR: connectivity references a node out of range!"; return false; }
-    }
-    for (int p = 0; p < NGLL; ++p) {
-      double xg = 0, yg = 0, zg = 0;
-      for (int g = 0; g < 8; ++g) {
-        xg = xg + shape[g][p] * x8[c[g]];
-        yg = yg + shape[g][p] * y8[c[g]];
-        zg = zg + shape[g][p] * z8[c[g]];
+  parallel_ranges((size_t)nelmt, host_threads(), [&](size_t e0, size_t e1) {
+    for (size_t e = e0; e < e1; ++e) {
+      int c[8];
+      for (int g = 0; g < 8; ++g) c[g] = conn8[e * 8 + g] - 1;
+      for (int p = 0; p < NGLL; ++p) {
+        double xg = 0, yg = 0, zg = 0;
+        for (int g = 0; g < 8; ++g) {
+          xg = xg + shape[g][p] * x8[c[g]];
+          yg = yg + shape[g][p] * y8[c[g]];
+          zg = zg + shape[g][p] * z8[c[g]];
+        }
+        const size_t q = e * NGLL + p;
+        xs[q] = xg; ys[q] = yg; zs[q] = zg;
       }
-      size_t q = (size_t)e * NGLL + p;
-      xs[q] = xg; ys[q] = yg; zs[q] = zg;
     }
-  }
+  });
   // Merge: order points by (x, y, z) with the reference's segment-by-segment
   // tolerance scheme; a new point starts where any coordinate jumps by more
   // than tol relative to the previous point in the final order.
   const double tol = 1.e-10 * std::fabs(xmax - xmin);
-  std::vector<int> order(np);
-  std::iota(order.begin(), order.end(), 0);
-  std::vector<char> seg(np, 0);
-  seg[0] = 1;
+  std::vector<int> order;
+  std::vector<char> seg;
   const std::vector<double>* keys[3] = {&xs, &ys, &zs};
-  for (int d = 0; d < 3; ++d) {
-    const std::vector<double>& key = *keys[d];
-    size_t a = 0;
-    while (a < np) {
-      size_t b = a + 1;
-      while (b < np && !seg[b]) ++b;
-      std::stable_sort(order.begin() + a, order.begin() + b,
-                       [&](int p, int q) { return key[p] < key[q]; });
-      a = b;
-    }
-    for (size_t i = 1; i < np; ++i)
-      if (std::fabs(key[order[i]] - key[order[i - 1]]) > tol) seg[i] = 1;
-  }
+  merge_order(keys, np, tol, order, seg);
   std::vector<int> iglob(np);
   int ig = 0;
   for (size_t i = 0; i < np; ++i) {

@@ -86,3 +86,28 @@ def test_bad_decks(tmp_path):
     bad = tmp_path / "nocontrol.sem"
     bad.write_text("\n".join(l for l in text.splitlines() if not l.startswith("control:")) + "\n")
     assert 'cannot read the "control:" line' in _err(str(bad))
+
+
+def test_tolerance_merge_of_duplicate_nodes(tmp_path):
+    """get_global merges points within 1e-10 |xmax - xmin| of each other
+    (src/mesh_spec.f90:146-262).  Here the mesh is big enough for the threaded
+    merge (several sorted chunks), and every third element refers to its own
+    jittered copies of its corner nodes.  Node numbering, coordinates and dof
+    maps equal the oracle's sequential merge."""
+    mesh = meshgen.box(nx=20, ny=20, nz=14, L=20.0, W=20.0, zbot=0.0, ztop=14.0)
+    rng = np.random.default_rng(7)
+    tol = 1e-10 * 20.0
+    x, y, z = list(mesh.x), list(mesh.y), list(mesh.z)
+    conn = mesh.conn.copy()
+    for e in range(0, mesh.nelmt, 3):
+        for g in range(8):
+            n = conn[e, g] - 1
+            j = rng.uniform(-0.3, 0.3, 3) * tol
+            x.append(mesh.x[n] + j[0]); y.append(mesh.y[n] + j[1]); z.append(mesh.z[n] + j[2])
+            conn[e, g] = len(x)
+    mesh.x, mesh.y, mesh.z, mesh.conn = np.array(x), np.array(y), np.array(z), conn
+    assert mesh.nelmt * 27 >= 2 * 65536
+    deck = meshgen.write_deck(mesh, str(tmp_path))
+    r = sg.read_deck(deck)
+    _same_mesh(r, OracleModel(deck=deck))
+    assert r["nnode"] == 41 * 41 * 29                 # the copies merged away
