@@ -607,7 +607,8 @@ class Model:
 
 
 class Server:
-    """sg_server: a request loop of factor-of-safety solves (see include/sg_solver.h)."""
+    """sg_server: a request loop of factor-of-safety and staged-excavation solves
+    (see include/sg_solver.h)."""
 
     def __init__(self, device: int = 0, hbm_budget: int = 0, workers: int = 4):
         self.h = lib().sg_server_create(device, hbm_budget, workers)
