@@ -55,3 +55,31 @@ def test_no_device_is_reported_not_faked(built_lib):
     with pytest.raises(sg.SgError):
         sg.Context(0)
     del ctypes
+
+
+def declared_prototypes():
+    """{name: number of parameters} of every function declared in the header."""
+    with open(os.path.join(ROOT, "include", "sg_solver.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(sg_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_the_header(built_lib):
+    """Every entry point the Python mirror declares argtypes for takes the
+    header's number of parameters (a miscount would pass garbage through the C ABI)."""
+    L = sg.lib()
+    protos = declared_prototypes()
+    assert set(protos) == set(declared_symbols())
+    checked = 0
+    for name, nargs in protos.items():
+        argtypes = getattr(getattr(L, name), "argtypes", None)
+        if argtypes is None:
+            continue
+        assert len(argtypes) == nargs, (name, len(argtypes), nargs)
+        checked += 1
+    assert checked >= len(protos) - 3   # all but argument-less calls carry argtypes
