@@ -131,3 +131,31 @@ def test_pore_pressure_weakens_the_slope(tmp_path):
     r_wet = wet.trial(1.2)
     assert r_wet["fmax"] > r_dry["fmax"]
     assert r_wet["umax"] > r_dry["umax"]
+
+
+def test_inclined_table_given_right_to_left(tmp_path):
+    """rx1 > rx2: the covered range is [min, max] and z interpolates from rx1."""
+    mesh = meshgen.slope2d(srf=(1.0,))
+    om = OracleModel(mesh)
+    om.set_water([1], _write(tmp_path, "1\n1\n1 20.0 0.0 7.0 3.0\n"))
+    wp, _ = om.pore_pressure()
+    c = _coords(om)
+    zs = 7.0 + (3.0 - 7.0) * (c[:, 0] - 20.0) / (0.0 - 20.0)
+    covered = c[:, 2] <= 7.0
+    assert np.array_equal(wp, np.where(covered & (zs > c[:, 2]), GAMW * (zs - c[:, 2]), 0.0))
+
+
+def test_vertical_meshed_face_takes_its_top(tmp_path):
+    """A vertical face (C = 0 in the plane equation) sets the surface at the
+    face's highest corner; its bounding box in x is a single plane."""
+    mesh = meshgen.box(nx=2, ny=2, nz=2, L=2.0, W=2.0, zbot=0.0, ztop=2.0)
+    faces = [(i + 2 * (j + 2 * k) + 1, meshgen.FACE_XMAX) for k in range(2) for j in range(2) for i in (1,)]
+    om = OracleModel(mesh)
+    om.set_water([1], _write(tmp_path, "1\n2\n%d\n" % len(faces) + "".join("%d %d\n" % f for f in faces)))
+    wp, _ = om.pore_pressure()
+    c = _coords(om)
+    on_plane = c[:, 0] == 2.0
+    # the first face (lower element) covers the plane's nodes up to its top z = 1; the
+    # upper element's face covers the rest with top z = 2
+    ztop = np.where(c[:, 2] <= 1.0, 1.0, 2.0)
+    assert np.array_equal(wp, np.where(on_plane, GAMW * (ztop - c[:, 2]), 0.0))
