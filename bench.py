@@ -161,7 +161,7 @@ def oracle_sample(n_cg: float = N_CG_REF, iters: int = 30):
     st = np.zeros(om.nelmt * 27 * 6)
     bl = np.zeros(om.neq + 1)
     t0 = time.perf_counter()
-    olib().orc_stress_update(om.h, u, ym, nu, phi, coh, psi, 1e-5, 0, 0, ev, st, bl)
+    om.stress_update(u, ym, nu, phi, coh, psi, 1e-5, 0, 0, ev, st, bl)
     t_st = time.perf_counter() - t0
     se = full["nelmt"] / om.nelmt
     t_nl = n_cg * t_pcg * se + t_st * se
