@@ -3,8 +3,9 @@
 The reference ships no tests or golden outputs and cannot be compiled here,
 so the oracle is pinned by analytic answers: the NGLL=3 GLL tables, the
 element matrix's rigid-body null space and symmetry, the exact confined
-gravity column, stress invariants at the Lode corners and Mohr-Coulomb
-yield values computed by hand.
+gravity column, the exact stress of an affine displacement on distorted
+elements, the overburden closed form, stress invariants at the Lode corners
+and Mohr-Coulomb yield values computed by hand.
 """
 import json
 import math
@@ -254,3 +255,73 @@ def test_pseudo_static_load_known_answer():
     np.testing.assert_allclose(g1[dofs[:, 1]], -0.05 * gz, rtol=1e-12)
     np.testing.assert_allclose(g1[dofs[:, 2]], 0.98 * gz, rtol=1e-12)
     assert np.all(g0[dofs[:, 0]] == 0) and np.all(g0[dofs[:, 1]] == 0)
+
+
+def _free_distorted_box(seed=11):
+    """2x2x2 box with its interior and top nodes moved (valid, non-parallelepiped
+    elements) and no constraints, so every node carries three free dofs."""
+    mesh = meshgen.box(nx=2, ny=2, nz=2, L=2.0, W=2.0, zbot=0.0, ztop=2.0,
+                       props=(20.0, 1e5, 0.3, 30.0, 1e9, 0.0))
+    rng = np.random.default_rng(seed)
+    move = mesh.z > 0.5
+    for a in (mesh.x, mesh.y, mesh.z):
+        a[move] += rng.uniform(-0.15, 0.15, move.sum())
+    mesh.bc = [np.zeros((0, 2), np.int32) for _ in range(3)]
+    return mesh
+
+
+def _affine_x(om, A, b):
+    a = om.arrays()
+    x = np.zeros(om.neq + 1)
+    u = a["g_coord"] @ A.T + b
+    x[a["gdof"].reshape(-1)] = u.reshape(-1)
+    return x
+
+
+def test_affine_displacement_gives_exact_elastic_stress():
+    """u = A X + b: a trilinear-mapped 27-node element reproduces it exactly,
+    so every GLL point of every (distorted) element has the strain sym(A) in
+    the reference's order (xx yy zz, engineering xy yz zx) and sigma = C eps
+    (src/postprocess.f90:40-79, src/preprocess.f90:12-68)."""
+    mesh = _free_distorted_box()
+    om = OracleModel(mesh)
+    assert om.neq == 3 * om.nnode
+    rng = np.random.default_rng(5)
+    A = 1e-3 * rng.standard_normal((3, 3))
+    x = _affine_x(om, A, np.array([0.1, -0.2, 0.05]))
+    eps = np.array([A[0, 0], A[1, 1], A[2, 2], A[0, 1] + A[1, 0], A[1, 2] + A[2, 1], A[2, 0] + A[0, 2]])
+    E, nu = 1e5, 0.3
+    f = E / ((1 + nu) * (1 - 2 * nu))
+    C = np.zeros((6, 6))
+    C[:3, :3] = f * nu
+    np.fill_diagonal(C[:3, :3], f * (1 - nu))
+    C[3:, 3:] = np.eye(3) * E / (2 * (1 + nu))
+    sig = C @ eps
+    st = np.zeros(om.nelmt * 27 * 6)
+    L.orc_elastic_stress(om.h, x, st)
+    np.testing.assert_allclose(st.reshape(-1, 6), np.broadcast_to(sig, (om.nelmt * 27, 6)),
+                               rtol=0, atol=1e-10 * np.abs(sig).max())
+    # the plastic block stores the same stress when nothing yields (c = 1e9):
+    # no plastic strain, no body load, fmax = 0
+    ev, st2, bl = np.zeros_like(st), np.zeros_like(st), np.zeros(om.neq + 1)
+    p = mesh.props[0]
+    fmax = om.stress_update(x, [p[1]], [p[2]], [p[3]], [p[4]], [p[5]], 1e-5, 1, 1, ev, st2, bl)
+    assert fmax == 0.0 and not ev.any() and not bl.any()
+    np.testing.assert_allclose(st2, st, rtol=0, atol=1e-12 * np.abs(sig).max())
+
+
+def test_overburden_stress_closed_form():
+    """sigma_zz = p0 - gamma |z - z0|, sigma_xx = sigma_yy = k0 sigma_zz at each
+    GLL point's node (src/postprocess.f90:10-33)."""
+    mesh = meshgen.excavation(nx=4, ny=4, nz=3, L=8.0, H=6.0, pit=4.0, lifts=1, lift_h=2.0)
+    om = OracleModel(mesh)
+    a = om.arrays()
+    st = np.zeros(om.nelmt * 27 * 6)
+    L.orc_overburden_stress(om.h, 6.0, -5.0, 0.5, st)
+    z = a["g_coord"][a["g_num"], 2]                              # (nelmt, 27)
+    gam = mesh.props[a["mat_id"] - 1, 0][:, None]
+    szz = -5.0 - gam * np.abs(z - 6.0)
+    st = st.reshape(om.nelmt, 27, 6)
+    assert np.array_equal(st[..., 2], szz)
+    assert np.array_equal(st[..., 0], 0.5 * szz) and np.array_equal(st[..., 1], 0.5 * szz)
+    assert not st[..., 3:].any()
