@@ -325,3 +325,43 @@ def test_overburden_stress_closed_form():
     assert np.array_equal(st[..., 2], szz)
     assert np.array_equal(st[..., 0], 0.5 * szz) and np.array_equal(st[..., 1], 0.5 * szz)
     assert not st[..., 3:].any()
+
+
+def test_strength_reduction_and_time_step_closed_form():
+    """c/SRF, atan(tan(phi)/SRF), atan(tan(psi)/SRF); the phi-nu correction of
+    Zheng et al. (2005) only where sin(phif) < 1 - 2 nu; dt = 4 (1+nu)(1-2nu) /
+    (E (1 - 2nu + sin^2 phif)) minimised over blocks
+    (src/plastic_library.f90:17-88)."""
+    from oracle.pyoracle import dt_viscoplas, strength_reduction
+    coh = np.array([10.0, 25.0, 5.0])
+    nu = np.array([0.3, 0.45, 0.2])
+    phi = np.array([20.0, 30.0, 40.0])
+    psi = np.array([0.0, 10.0, 5.0])
+    ym = np.array([1e5, 5e4, 2e5])
+    srf = 1.6
+    d = math.pi / 180.0
+    ist, cohf, nuf, phif, psif = strength_reduction(srf, coh, nu, phi, psi)
+    assert ist == 0 and np.array_equal(nuf, nu)
+    np.testing.assert_allclose(cohf, coh / srf, rtol=1e-15)
+    np.testing.assert_allclose(phif, np.degrees(np.arctan(np.tan(phi * d) / srf)), rtol=1e-14)
+    np.testing.assert_allclose(psif, np.degrees(np.arctan(np.tan(psi * d) / srf)), rtol=1e-14, atol=1e-15)
+    # unit SRF leaves everything unchanged
+    ist1, c1, n1, p1, q1 = strength_reduction(1.0, coh, nu, phi, psi)
+    assert ist1 == 0 and np.array_equal(c1, coh) and np.array_equal(p1, phi) and np.array_equal(q1, psi)
+    # phi-nu correction: blocks 0 and 2 have sin(phif) < 1 - 2 nu and are corrected,
+    # block 1 (nu = 0.45, 1 - 2 nu = 0.1) is not
+    ist2, _, nu2, phif2, _ = strength_reduction(srf, coh, nu, phi, psi, phinu=1)
+    assert ist2 == 1 and nu2[1] == nu[1] and nu2[0] != nu[0] and nu2[2] != nu[2]
+    for b in range(3):
+        om2 = 1 - 2 * nu[b]
+        snf = math.sin(phif2[b] * d)
+        if snf < om2:
+            beta = max(math.sin(phi[b] * d) / om2, 1.0 + 1e-12)
+            assert abs(nu2[b] - 0.5 * (1 - snf / beta)) <= 1e-15
+        else:
+            assert nu2[b] == nu[b]
+    assert ist2 == int(any(math.sin(phif2[b] * d) < 1 - 2 * nu[b] for b in range(3)))
+    dt = dt_viscoplas(nuf, phif, ym)
+    ref = min(4 * (1 + nuf[b]) * (1 - 2 * nuf[b]) / (ym[b] * (1 - 2 * nuf[b] + math.sin(phif[b] * d) ** 2))
+              for b in range(3))
+    assert abs(dt - ref) <= 1e-15 * ref
