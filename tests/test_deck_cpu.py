@@ -111,3 +111,19 @@ def test_tolerance_merge_of_duplicate_nodes(tmp_path):
     r = sg.read_deck(deck)
     _same_mesh(r, OracleModel(deck=deck))
     assert r["nnode"] == 41 * 41 * 29                 # the copies merged away
+
+
+def test_psem_deck_reads_its_unpartitioned_inputs(tmp_path):
+    """A .psem deck names nproc, part_path and a ghost file for the MPI build;
+    the single-GPU reader ignores them and reads the same input files."""
+    mesh = meshgen.slope2d(srf=(1.0, 1.5))
+    deck = meshgen.write_deck(mesh, str(tmp_path))
+    text = open(deck).read()
+    text = text.replace("preinfo: ", "preinfo: nproc=4, part_path='./partition', ")
+    text = text.replace("idfile='slope2d_material_id'", "idfile='slope2d_material_id', gfile='slope2d_ghost'")
+    assert "nproc=4" in text and "gfile=" in text
+    psem = tmp_path / "slope2d.psem"
+    psem.write_text(text)
+    a, b = sg.read_deck(deck), sg.read_deck(str(psem))
+    for k in ("g_coord", "g_num", "gdof", "gdof_elmt", "mat_id", "props", "srf"):
+        assert np.array_equal(a[k], b[k]), k
