@@ -443,8 +443,11 @@ bool read_deck(const char* path, HostMesh& M, std::vector<double>& x8, std::vect
       int bctype;
       double val;
       while (f >> bctype >> val) {
+        // the reference's checks and messages (src/apply_bc.f90:36-60)
         if (val != 0.0) { err = "ERROR: nonzero displacement BC not implemented!"; return false; }
-        if (bctype != 2) { err = "ERROR: only face displacement BCs are implemented!"; return false; }
+        if (bctype == 0) { err = "ERROR: nodal displacement BC not implemented!"; return false; }
+        if (bctype == 1) { err = "ERROR: edge displacement BC not implemented!"; return false; }
+        if (bctype != 2) { err = "ERROR: undefined displacement BC type ux! " + std::to_string(bctype); return false; }
         int nel;
         f >> nel;
         for (int i = 0; i < nel; ++i) {

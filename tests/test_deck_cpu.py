@@ -83,6 +83,16 @@ def test_bad_decks(tmp_path):
     bad = tmp_path / "water.sem"
     bad.write_text(text + "water: wsfile='ws'\n")     # no water IDs after the material blocks
     assert "water IDs cannot be read from material list" in _err(str(bad))
+    # boundary-condition types the reference rejects, with its messages (src/apply_bc.f90:36-60)
+    bcfile = tmp_path / "slope2d_ssbcux"
+    good_bc = bcfile.read_text()
+    for head, msg in (("2 0.5", "nonzero displacement BC not implemented"),
+                      ("0 0.0", "nodal displacement BC not implemented"),
+                      ("1 0.0", "edge displacement BC not implemented"),
+                      ("7 0.0", "undefined displacement BC type")):
+        bcfile.write_text(head + "\n" + good_bc.split("\n", 1)[1])
+        assert msg in _err(deck), head
+    bcfile.write_text(good_bc)
     bad = tmp_path / "nocontrol.sem"
     bad.write_text("\n".join(l for l in text.splitlines() if not l.startswith("control:")) + "\n")
     assert 'cannot read the "control:" line' in _err(str(bad))
