@@ -368,9 +368,21 @@ bool read_deck(const char* path, HostMesh& M, std::vector<double>& x8, std::vect
       if (eq != std::string::npos) kv[trim(arg.substr(0, eq))] = unquote(arg.substr(eq + 1));
     }
   }
-  for (const char* need : {"preinfo:", "mesh:", "bc:", "material:", "control:"})
-    if (!L.count(need)) { err = std::string("ERROR: cannot read the \"") + need + "\" line!"; return false; }
+  // required lines, with the reference's messages (src/read_input.f90:409-442)
+  static const char* need[][2] = {{"preinfo:", "pre"}, {"mesh:", "mesh"}, {"bc:", "BC"},
+                                  {"material:", "material"}, {"control:", "control"}};
+  for (auto& nd : need)
+    if (!L.count(nd[0])) {
+      err = std::string("ERROR: cannot read ") + nd[1] + " information! make sure the line with \"" + nd[0] +
+            "\" token is correct.";
+      return false;
+    }
   auto& pre = L["preinfo:"];
+  {  // src/read_input.f90:173-180
+    const std::string method = pre.count("method") ? pre["method"] : "";
+    if (method == "fem") { err = "ERROR: only method='sem' is supported!"; return false; }
+    if (method != "sem") { err = "ERROR: wrong value for method!"; return false; }
+  }
   if (pre["ngllx"] != "3" || pre["nglly"] != "3" || pre["ngllz"] != "3") {
     err = "ERROR: only ngllx=nglly=ngllz=3 is supported!"; return false;
   }

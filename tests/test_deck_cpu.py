@@ -95,7 +95,10 @@ def test_bad_decks(tmp_path):
     bcfile.write_text(good_bc)
     bad = tmp_path / "nocontrol.sem"
     bad.write_text("\n".join(l for l in text.splitlines() if not l.startswith("control:")) + "\n")
-    assert 'cannot read the "control:" line' in _err(str(bad))
+    assert 'cannot read control information! make sure the line with "control:" token is correct' in _err(str(bad))
+    bad = tmp_path / "method.sem"
+    bad.write_text(text.replace("method='sem'", "method='xyz'"))
+    assert "wrong value for method" in _err(str(bad))
 
 
 def test_tolerance_merge_of_duplicate_nodes(tmp_path):
