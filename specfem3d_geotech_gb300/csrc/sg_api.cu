@@ -57,6 +57,7 @@ struct sg_ctx {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
   std::vector<std::pair<int, int>> ev_used;  // (pool index, category)
   double* pin = nullptr;                     // pinned scratch for scalars
+  int* d_err = nullptr;  // bounded-wait error word of this context's applies outside a PCG solve
   cudaEvent_t marks[16] = {};
   long long launch0 = 0;
   int* d_nbr = nullptr;
@@ -246,7 +247,8 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
   int ev;
   if (!(mode & 4)) {  // bit 2: the caller guarantees u = 0, so kp = K u = 0 without an apply
     ev = C->prof_begin();
-    pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, u, (const V*)nullptr, 0, B.Y, B.cs, B.G, C->d_nbr, op.T->d_pos, s);
+    pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, u, (const V*)nullptr, 0, B.Y, B.cs, B.G, C->d_nbr, op.T->d_pos,
+                     &B.G->err, s);
     C->prof_end(ev, 1);
     pcg_gather<V, KR>(*op.T, B.Y, B.kp, B.p, B.z, 0, B.cs, B.G, B.part, s);
   }
@@ -261,7 +263,8 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
   auto eager_chunk = [&]() {
     for (int c = 0; c < chunk; ++c) {
       ev = C->prof_begin();
-      pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, B.p, B.z, 1, B.Y, B.cs, B.G, C->d_nbr, op.T->d_pos, s);
+      pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, B.p, B.z, 1, B.Y, B.cs, B.G, C->d_nbr, op.T->d_pos,
+                       &B.G->err, s);
       C->prof_end(ev, 1);
       ev = C->prof_begin();
       pcg_gather<V, KR>(*op.T, B.Y, B.kp, B.p, B.z, 1, B.cs, B.G, B.part, s);
@@ -306,6 +309,12 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
     cudaMemcpyAsync((void*)hG, B.G, sizeof(PcgGlobal), cudaMemcpyDeviceToHost, s);
     if (!C->check(cudaStreamSynchronize(s), "pcg")) return SG_ERR_CUDA;
     it = hG->it;
+    if (hG->err) {
+      // a bounded wait of this solve ran out: stop before another chunk
+      status = SG_ERR_TIMEOUT;
+      C->err = "PCG: a bounded wait timed out";
+      break;
+    }
     if (hG->all_done) break;
     if (it >= maxiter + chunk) { status = SG_ERR_TIMEOUT; break; }
     double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -343,11 +352,11 @@ template <typename V>
 static void apply_plain(sg_ctx* C, int KR, const Op& op, const V* x, V* Y, V* out) {
   int ev = C->prof_begin();
   switch (KR) {
-    case 1: pcg_apply<V, 1>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
-    case 2: pcg_apply<V, 2>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
-    case 4: pcg_apply<V, 4>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
-    case 8: pcg_apply<V, 8>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
-    case 16: pcg_apply<V, 16>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->stream); break;
+    case 1: pcg_apply<V, 1>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->d_err, C->stream); break;
+    case 2: pcg_apply<V, 2>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->d_err, C->stream); break;
+    case 4: pcg_apply<V, 4>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->d_err, C->stream); break;
+    case 8: pcg_apply<V, 8>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->d_err, C->stream); break;
+    case 16: pcg_apply<V, 16>(op.dense, op.K, op.ge, op.nelmt, x, (const V*)nullptr, 0, Y, nullptr, nullptr, C->d_nbr, op.T->d_pos, C->d_err, C->stream); break;
   }
   C->prof_end(ev, 1);
   ev = C->prof_begin();
@@ -387,6 +396,8 @@ sg_ctx* sg_create(int device, size_t hbm_budget) {
   const KsTables& T = ks_tables();
   c->d_nbr = c->alloc<int>(NGLL * KS_NBR);
   c->d_entry = c->alloc<int>(KS_NNZ);
+  c->d_err = c->alloc<int>(1);
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   cudaMemcpy(c->d_nbr, T.nbr, sizeof(T.nbr), cudaMemcpyHostToDevice);
   cudaMemcpy(c->d_entry, T.entry, sizeof(T.entry), cudaMemcpyHostToDevice);
   set_entry_table(c->d_entry);
@@ -1305,9 +1316,17 @@ static int batch_iteration(sg_model* M) {
     S.res.failed = (S.res.nl_iter == ctl->nl_maxiter);
     slot_finish(M, t);
   }
-  if (apply_error_flag(s) || apply_tc_error_flag(s) || apply_lanes_error_flag(s) || persist_error_flag(s)) {
-    c->err = "element apply: a bounded wait timed out";
-    return SG_ERR_TIMEOUT;
+  {
+    // the applies outside the PCG solves (refinement residuals) report to the
+    // context's error word; it is cleared once read
+    int* herr = (int*)c->pin;
+    cudaMemcpyAsync(herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (!c->check(cudaStreamSynchronize(s), "plastic iteration")) return SG_ERR_CUDA;
+    if (*herr) {
+      cudaMemsetAsync(c->d_err, 0, sizeof(int), s);
+      c->err = "element apply: a bounded wait timed out";
+      return SG_ERR_TIMEOUT;
+    }
   }
   return c->check(cudaGetLastError(), "plastic iteration") ? SG_OK : SG_ERR_CUDA;
 }

@@ -18,8 +18,8 @@
 // element slots of a stage fall on distinct 16-byte bank groups.  The next
 // group's dof numbers and gather positions travel to shared memory by
 // cp.async while the current group computes.  Every wait
-// is bounded; a timeout sets a device flag, the warp drains its own copies
-// (bounded) and stops.
+// is bounded; a timeout sets the caller's error word, the warp drains its own
+// copies (bounded) and stops.
 //
 // Sums per output entry run in storage order, so results are deterministic
 // (bitwise equal from run to run) but round differently from the per-node
@@ -66,8 +66,6 @@ constexpr BlockTable make_blocks() {
 }
 constexpr BlockTable BT = make_blocks();
 static_assert(BT.count * 9 == KS_NNZ, "270 stored node blocks");
-
-__device__ int g_lanes_err;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -190,7 +188,7 @@ template <int KR>
 __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
     const float* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const float* __restrict__ pold,
     const float* __restrict__ z, int combine, float* __restrict__ Y, const ColState* __restrict__ cs,
-    const PcgGlobal* __restrict__ G, const int* __restrict__ pos) {
+    const PcgGlobal* __restrict__ G, const int* __restrict__ pos, int* __restrict__ err) {
   using S = Shape<KR>;
   if (G && G->all_done) return;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -252,7 +250,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
       // shared __syncwarp sequence alone
       const bool w = __all_sync(0xffffffffu, mbar_wait(bar + (C % NSTAGE), (unsigned)((C / NSTAGE) & 1)));
       if (!w) {
-        if (lane == 0) atomicExch(&g_lanes_err, 1);
+        if (lane == 0) atomicExch(err, 1);
         ok = false;
         return;
       }
@@ -287,7 +285,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
 
 template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
-                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, cudaStream_t s) {
+                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s) {
   using S = lanes::Shape<KR>;
   static bool attr = false;
   if (!attr) {
@@ -298,23 +296,16 @@ void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* 
   const int warps = (ngroups + lanes::NW - 1) / lanes::NW;
   int grid = warps < 152 ? warps : 152;
   if (grid < 1) return;
-  lanes::k_apply_lanes<KR><<<grid, lanes::NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, combine, Y, cs, G, pos);
+  lanes::k_apply_lanes<KR><<<grid, lanes::NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, combine, Y, cs, G, pos, err);
 }
 
 size_t apply_lanes_smem(int KR) {
   return KR == 8 ? lanes::Shape<8>::SMEM : KR == 16 ? lanes::Shape<16>::SMEM : lanes::Shape<4>::SMEM;
 }
 
-int apply_lanes_error_flag(cudaStream_t s) {
-  int h = 0;
-  cudaMemcpyFromSymbolAsync(&h, lanes::g_lanes_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
-  cudaStreamSynchronize(s);
-  return h;
-}
-
 template void launch_apply_lanes<8>(const float*, const int*, int, const float*, const float*, int, float*,
-                                    const ColState*, const PcgGlobal*, const int*, cudaStream_t);
+                                    const ColState*, const PcgGlobal*, const int*, int*, cudaStream_t);
 template void launch_apply_lanes<16>(const float*, const int*, int, const float*, const float*, int, float*,
-                                     const ColState*, const PcgGlobal*, const int*, cudaStream_t);
+                                     const ColState*, const PcgGlobal*, const int*, int*, cudaStream_t);
 
 }  // namespace sg

@@ -52,7 +52,6 @@ constexpr uint32_t TMEM_COLS = 32;                     // two 16-column accumula
 // N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 constexpr uint32_t IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((128u >> 4) << 24);
 
-__device__ int g_tc_err;
 
 // KR consecutive floats with 16-byte loads
 template <int KR>
@@ -141,7 +140,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_apply_tc(const float* __restrict
                                                           int nelmt, const float* __restrict__ pold,
                                                           const float* __restrict__ z, int combine, float* __restrict__ Y,
                                                           const ColState* __restrict__ cs, const PcgGlobal* __restrict__ G,
-                                                          const int* __restrict__ entry_g, const int* __restrict__ pos) {
+                                                          const int* __restrict__ entry_g, const int* __restrict__ pos,
+                                                          int* __restrict__ err) {
   if (G && G->all_done) return;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-byte aligned working base (the 128B swizzle pattern uses address bits 7-9)
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_apply_tc(const float* __restrict
       }
     }
   }
-  if (fault && tid == 0) atomicExch(&g_tc_err, 1);
+  if (fault && tid == 0) atomicExch(err, 1);
   // drain what is still in flight (bounded), then free TMEM
   if (tid == 0) {
     for (int i = kwaited; i < issued; ++i) mbar_wait(&kbar[i & 1], (unsigned)((i >> 1) & 1));
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_apply_tc(const float* __restrict
 template <int KR>
 void launch_apply_tc(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
                      float* Y, const ColState* cs, const PcgGlobal* G, const int* d_entry, const int* pos,
-                     cudaStream_t s) {
+                     int* err, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(tc::k_apply_tc<KR>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
@@ -333,19 +333,12 @@ void launch_apply_tc(const float* Ks, const int* ge, int nelmt, const float* pol
   int grid = nelmt < 152 ? nelmt : 152;
   if (grid < 1) return;
   tc::k_apply_tc<KR><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(Ks, ge, nelmt, pold, z, combine, Y, cs, G, d_entry,
-                                                               pos);
-}
-
-int apply_tc_error_flag(cudaStream_t s) {
-  int h = 0;
-  cudaMemcpyFromSymbolAsync(&h, tc::g_tc_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
-  cudaStreamSynchronize(s);
-  return h;
+                                                               pos, err);
 }
 
 template void launch_apply_tc<8>(const float*, const int*, int, const float*, const float*, int, float*,
-                                 const ColState*, const PcgGlobal*, const int*, const int*, cudaStream_t);
+                                 const ColState*, const PcgGlobal*, const int*, const int*, int*, cudaStream_t);
 template void launch_apply_tc<16>(const float*, const int*, int, const float*, const float*, int, float*,
-                                  const ColState*, const PcgGlobal*, const int*, const int*, cudaStream_t);
+                                  const ColState*, const PcgGlobal*, const int*, const int*, int*, cudaStream_t);
 
 }  // namespace sg

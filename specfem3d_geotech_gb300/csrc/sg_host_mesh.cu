@@ -378,9 +378,11 @@ bool read_deck(const char* path, HostMesh& M, std::vector<double>& x8, std::vect
       return false;
     }
   auto& pre = L["preinfo:"];
-  {  // src/read_input.f90:173-180
-    const std::string method = pre.count("method") ? pre["method"] : "";
-    if (method == "fem") { err = "ERROR: only method='sem' is supported!"; return false; }
+  {  // method defaults to sem and a blank value keeps it (src/read_input.f90:87,161-162,173-180)
+    const std::string method = (pre.count("method") && !trim(pre["method"]).empty()) ? trim(pre["method"]) : "sem";
+    // the reference accepts fem; this solve path is spectral only (a
+    // limitation of this library, not a reference message)
+    if (method == "fem") { err = "ERROR: method='fem' is not supported by this solver (method='sem' only)!"; return false; }
     if (method != "sem") { err = "ERROR: wrong value for method!"; return false; }
   }
   if (pre["ngllx"] != "3" || pre["nglly"] != "3" || pre["ngllz"] != "3") {

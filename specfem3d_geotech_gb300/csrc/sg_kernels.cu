@@ -540,7 +540,6 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse(
 // the current one, so the HBM stream overlaps the shared-memory matvec.
 // Every wait is bounded: on timeout the kernel records the fault in *err and
 // the warp stops after draining its own copies (also bounded).
-__device__ int g_apply_err;  // set to 1 by a timed-out mbarrier wait
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -575,7 +574,8 @@ template <typename V, int KR>
 __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
     const V* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const V* __restrict__ pold,
     const V* __restrict__ z, int combine, V* __restrict__ Y, const ColState* __restrict__ cs,
-    const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g, const int* __restrict__ pos) {
+    const PcgGlobal* __restrict__ G, const int* __restrict__ nbr_g, const int* __restrict__ pos,
+    int* __restrict__ err) {
   if (G && G->all_done) return;
   extern __shared__ __align__(128) unsigned char smem[];
   // p tile: one row of 3*KR values per node, padded so that node rows start
@@ -634,7 +634,7 @@ __global__ void __launch_bounds__(APPLY_WARPS * 32) k_apply_sparse_tma(
     bool ok = mbar_wait(bar + (i & 1), (unsigned)((i >> 1) & 1));
     ++waited;
     if (!ok) {
-      if (lane == 0) atomicExch(&g_apply_err, 1);
+      if (lane == 0) atomicExch(err, 1);
       break;
     }
     __syncwarp();
@@ -718,13 +718,6 @@ static size_t apply_tma_smem() {
   return 3072 + (size_t)APPLY_WARPS * (2 * KS_STRIDE + ((NGLL * PROW + 3) & ~3)) * sizeof(V);
 }
 
-int apply_error_flag(cudaStream_t s) {
-  int h = 0;
-  cudaMemcpyFromSymbolAsync(&h, g_apply_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
-  cudaStreamSynchronize(s);
-  return h;
-}
-
 template <typename V, int KR>
 static size_t apply_sparse_smem() {
   return 2064 + (size_t)APPLY_WARPS * (KS_STRIDE + ((NEDOF * KR + 3) & ~3)) * sizeof(V);
@@ -732,7 +725,7 @@ static size_t apply_sparse_smem() {
 
 template <typename V, int KR>
 void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_old, const V* z, int combine, V* Y,
-               const ColState* cs, const PcgGlobal* G, const int* d_nbr, const int* pos, cudaStream_t s) {
+               const ColState* cs, const PcgGlobal* G, const int* d_nbr, const int* pos, int* err, cudaStream_t s) {
   if (nelmt <= 0) return;
   int blocks = (nelmt + APPLY_WARPS - 1) / APPLY_WARPS;
   if (dense == 2) {
@@ -748,11 +741,11 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
   }
   if constexpr (std::is_same<V, float>::value && (KR == 8 || KR == 16)) {
     if (g_apply_variant == 2) {
-      SG_LAUNCH launch_apply_tc<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, g_entry_dev, pos, s);
+      SG_LAUNCH launch_apply_tc<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, g_entry_dev, pos, err, s);
       return;
     }
     if (g_apply_variant >= 3) {
-      SG_LAUNCH launch_apply_lanes<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, pos, s);
+      SG_LAUNCH launch_apply_lanes<KR>((const float*)K, ge, nelmt, p_old, z, combine, Y, cs, G, pos, err, s);
       return;
     }
   }
@@ -768,7 +761,7 @@ void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_ol
     if (per_sm < 1) per_sm = 1;
     int grid = std::min(blocks, 152 * per_sm);
     SG_LAUNCH k_apply_sparse_tma<V, KR><<<grid, APPLY_WARPS * 32, sm, s>>>((const V*)K, ge, nelmt, p_old, z, combine, Y, cs,
-                                                                 G, d_nbr, pos);
+                                                                 G, d_nbr, pos, err);
     return;
   }
   size_t sm = apply_sparse_smem<V, KR>();
@@ -1986,7 +1979,7 @@ void launch_invert_diag(int n1, double* dprecon, float* dprecon32, cudaStream_t 
 // explicit instantiations
 #define SG_INST(V, KR)                                                                                          \
   template void pcg_apply<V, KR>(int, const void*, const int*, int, const V*, const V*, int, V*, const ColState*, \
-                                 const PcgGlobal*, const int*, const int*, cudaStream_t);                                   \
+                                 const PcgGlobal*, const int*, const int*, int*, cudaStream_t);                             \
   template void pcg_gather<V, KR>(const GatherTopo&, const V*, V*, V*, const V*, int, ColState*, PcgGlobal*,    \
                                   double*, cudaStream_t);                                                       \
   template void pcg_update<V, KR>(int, V*, V*, V*, const V*, const V*, const V*, const V*, int, ColState*,      \

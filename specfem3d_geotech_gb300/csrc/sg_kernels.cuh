@@ -28,6 +28,7 @@ struct PcgGlobal {
   int mode;       // bit 0: 0 = reference step test, 1 = residual reduction test; bit 1: keep direction
   int kcols;      // columns in use (<= KR)
   unsigned cntB, cntC, pad;
+  int err;        // set to 1 by a bounded wait of this solve's kernels that ran out
 };
 
 // Factored material block for the stress update, per trial.
@@ -46,16 +47,16 @@ void set_apply_variant(int v);   // 0 register-staged, 1 TMA pipeline, 2 tensor 
                                  // 3 lane per (element, RHS) for 8/16 FP32 RHS, 4 matrix-free FP32,
                                  // 5 (default) 3 with matrix-free FP32 on small meshes
 void set_entry_table(const int* d_entry);
-int apply_tc_error_flag(cudaStream_t s);
+// The element applies that wait on mbarriers set *err to 1 when a bounded
+// wait runs out (err is the calling solve's own word, never shared between
+// contexts).
 template <int KR>
 void launch_apply_tc(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
                      float* Y, const ColState* cs, const PcgGlobal* G, const int* d_entry, const int* pos,
-                     cudaStream_t s);
-int apply_error_flag(cudaStream_t s);  // 1 if an apply kernel timed out on an mbarrier
+                     int* err, cudaStream_t s);
 template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
-                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, cudaStream_t s);
-int apply_lanes_error_flag(cudaStream_t s);
+                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s);
 // Matrix-free FP32 apply (sg_apply_mf.cu): rec holds per GLL point J^-1 and the
 // C constants times w detJ; pcg_apply takes it with dense = 2.
 template <int KR>
@@ -75,13 +76,14 @@ bool launch_pcg_persistent(const float* rec, const int* ge, int nelmt, const int
                            ColState* cs, PcgGlobal* G, double* part, int chunk, cudaStream_t s);
 bool persist_enabled();                 // SG_PERSIST=0 turns the persistent chunk off
 int persist_max_elements();             // meshes below this use it
-int persist_error_flag(cudaStream_t s);  // 1 if a persistent chunk's grid barrier timed out  // the FP32 operator of the mixed solve is applied matrix-free
+// a persistent chunk whose grid barrier timed out sets G->err
 void set_gather_variant(int v);  // 1 row-cooperative gather for FP32 with 4/8/16 RHS (default), 0 staged
 template <typename V, int KR>
 // Y receives element slot (e, a)'s three rows (x KR) at the slot's gather
 // position pos[e*27+a] (slots of fully fixed nodes, pos < 0, are skipped).
 void pcg_apply(int dense, const void* K, const int* ge, int nelmt, const V* p_old, const V* z, int combine,
-               V* Y, const ColState* cs, const PcgGlobal* G, const int* d_nbr, const int* pos, cudaStream_t s);
+               V* Y, const ColState* cs, const PcgGlobal* G, const int* d_nbr, const int* pos, int* err,
+               cudaStream_t s);
 template <typename V, int KR>
 void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mode, ColState* cs,
                 PcgGlobal* G, double* part, cudaStream_t s);

@@ -24,6 +24,7 @@
 // after it completes.
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "sg_kernels.cuh"
 
@@ -35,6 +36,10 @@ constexpr size_t SG_NOALLOC_SCRATCH_BYTES = size_t(64) << 20;
 __device__ __align__(256) unsigned char g_noalloc_scratch[SG_NOALLOC_SCRATCH_BYTES];
 
 constexpr int MAX_DEVICES = 64;
+// Device address of the scratch array per device, looked up on the first call.
+// Written without a lock: two threads making their first call on one device
+// at the same time both store the same address, so the race is benign (and
+// their solves would race on the array anyway; the caller serialises them).
 unsigned char* g_scratch_addr[MAX_DEVICES] = {};
 
 void tag(char* errtag, const std::string& msg) {
@@ -148,6 +153,28 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
       return SG_ERR_BADARG;
     }
   const size_t n1 = (size_t)neq + 1, nslots = (size_t)nelmt * NGLL;
+  {
+    // The device builds one gather group per node, keyed by the node's
+    // smallest free dof, and takes the group's dof triple from any of its
+    // slots.  A dof map in which two slots share that key but not all three
+    // dofs is not a node numbering; reject it so that this call gives the same
+    // solve as sg_pcg_solve (host memory only).
+    std::vector<int> trip(3 * n1, -1);
+    for (size_t sl = 0; sl < nslots; ++sl) {
+      const int* g = gdof_elmt + 3 * sl;
+      int key = 0;
+      for (int d = 0; d < 3; ++d)
+        if (g[d] > 0 && (key == 0 || g[d] < key)) key = g[d];
+      if (!key) continue;
+      int* t = trip.data() + 3 * (size_t)key;
+      if (t[0] < 0) {
+        t[0] = g[0]; t[1] = g[1]; t[2] = g[2];
+      } else if (t[0] != g[0] || t[1] != g[1] || t[2] != g[2]) {
+        tag(errtag, "ERROR: gdof_elmt gives one dof to nodes with different dof triples!");
+        return SG_ERR_BADARG;
+      }
+    }
+  }
   // scratch layout
   size_t off = 0;
   auto take = [&](size_t bytes) { size_t o = off; off += up256(bytes); return o; };
@@ -252,7 +279,7 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
   cudaMemsetAsync(dP, 0, sizeof(double) * n1, s);
   cudaMemsetAsync(dKp, 0, sizeof(double) * n1, s);
   // kp = K u, r = f - kp, z = D r, p = z (src/solver.f90:38-50)
-  pcg_apply<double, 1>(1, dK, dGe, nelmt, dU, (const double*)nullptr, 0, dY, dCs, dG, nullptr, dPos, s);
+  pcg_apply<double, 1>(1, dK, dGe, nelmt, dU, (const double*)nullptr, 0, dY, dCs, dG, nullptr, dPos, &dG->err, s);
   pcg_gather<double, 1>(T, dY, dKp, dP, dZ, 0, dCs, dG, dPart, s);
   pcg_update<double, 1>((int)n1, dU, dR, dZ, dP, dKp, dF, dDp, 1, dCs, dG, dPart, s);
   const int chunk = 16;
@@ -260,7 +287,7 @@ extern "C" int sg_pcg_solve_noalloc(int neq, int nelmt, int nedof, const double*
   PcgGlobal got;
   for (;;) {
     for (int c = 0; c < chunk; ++c) {
-      pcg_apply<double, 1>(1, dK, dGe, nelmt, dP, dZ, 1, dY, dCs, dG, nullptr, dPos, s);
+      pcg_apply<double, 1>(1, dK, dGe, nelmt, dP, dZ, 1, dY, dCs, dG, nullptr, dPos, &dG->err, s);
       pcg_gather<double, 1>(T, dY, dKp, dP, dZ, 1, dCs, dG, dPart, s);
       pcg_update<double, 1>((int)n1, dU, dR, dZ, dP, dKp, dF, dDp, 0, dCs, dG, dPart, s);
     }

@@ -20,11 +20,12 @@
 // per-column stop tests are those of the update kernel (reference step test
 // of src/solver.f90:61-73 or the residual-reduction test).
 //
-// The barrier is bounded: a block that waits too long sets a device flag and
-// leaves; every other block's wait then runs out as well, the launch ends and
-// the solve reports SG_ERR_TIMEOUT.  The barrier's arrival count and
-// generation live in the solve's own control word, so concurrent solves on
-// other streams do not share it.
+// The barrier is bounded: a block that waits too long sets the error word of
+// the solve's control word and leaves; every other block's wait then runs out
+// as well, the launch ends and the solve reports SG_ERR_TIMEOUT without
+// launching another chunk.  The barrier's arrival count and generation live in
+// the solve's own control word (the count is zeroed before every launch), so
+// concurrent solves on other streams do not share them.
 #include <cstdint>
 #include <cstdlib>
 
@@ -36,8 +37,6 @@ namespace pp {
 
 constexpr int NT = 256;               // threads per block
 constexpr int BAR_TRIES = 1 << 20;    // bounded barrier wait (x ~64 ns)
-
-__device__ int g_persist_err;
 
 // compensated FP32 dot accumulator (exact products, two-float sum)
 struct CompSum {
@@ -72,7 +71,7 @@ __device__ __forceinline__ bool grid_barrier(PcgGlobal* G) {
       while (*gen == g0) {
         if (++tries > BAR_TRIES) {
           ok = 0;
-          atomicExch(&g_persist_err, 1);
+          atomicExch(&G->err, 1);
           break;
         }
         __nanosleep(64);
@@ -447,6 +446,9 @@ bool launch_pcg_persistent(const float* rec, const int* ge, int nelmt, const int
     if (grid < 1) return false;
     // the partial buffer holds NPART * 16 * 4 doubles
     if ((size_t)grid * KR * 5 > (size_t)NPART * 16 * 4) return false;
+    // a barrier count left behind by an earlier launch would release the
+    // first barrier early: start every launch from zero arrivals
+    cudaMemsetAsync(&G->cntB, 0, sizeof(unsigned), s);
     pp::Args A{rec, ge, nelmt, pos, T.d_ptr, T.d_dof, T.ngroups, n1, u, r, z, p, kp, Y, dp, cs, G, part, chunk};
     void* args[] = {&A};
     if (cudaLaunchCooperativeKernel((const void*)pp::k_pcg_persistent<KR>, grid, pp::NT, args, 0, s) !=
@@ -457,13 +459,6 @@ bool launch_pcg_persistent(const float* rec, const int* ge, int nelmt, const int
     add_launches(1);
     return true;
   }
-}
-
-int persist_error_flag(cudaStream_t s) {
-  int h = 0;
-  cudaMemcpyFromSymbolAsync(&h, pp::g_persist_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
-  cudaStreamSynchronize(s);
-  return h;
 }
 
 #define SG_PP_INST(KR)                                                                                              \

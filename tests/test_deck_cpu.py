@@ -99,6 +99,27 @@ def test_bad_decks(tmp_path):
     bad = tmp_path / "method.sem"
     bad.write_text(text.replace("method='sem'", "method='xyz'"))
     assert "wrong value for method" in _err(str(bad))
+    bad.write_text(text.replace("method='sem'", "method='fem'"))
+    assert "not supported by this solver" in _err(str(bad))
+
+
+def test_method_defaults_to_sem(tmp_path):
+    """method='sem' is the reference's default (src/read_input.f90:87); a
+    preinfo line without the key, or with a blank value, reads the same deck."""
+    mesh = meshgen.slope2d(srf=(1.0, 1.5))
+    deck = meshgen.write_deck(mesh, str(tmp_path))
+    text = open(deck).read()
+    assert "method='sem'" in text
+    a = sg.read_deck(deck)
+    for variant, repl in (("nomethod", ""), ("blank", "method=''")):
+        d = tmp_path / (variant + ".sem")
+        t = text.replace("method='sem', ", repl + (", " if repl else "")) if "method='sem', " in text \
+            else text.replace("method='sem'", repl)
+        assert ("method='sem'" not in t)
+        d.write_text(t)
+        b = sg.read_deck(str(d))
+        for k in ("g_coord", "g_num", "gdof", "gdof_elmt", "mat_id", "props", "srf"):
+            assert np.array_equal(a[k], b[k]), (variant, k)
 
 
 def test_tolerance_merge_of_duplicate_nodes(tmp_path):

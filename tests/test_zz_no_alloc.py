@@ -52,6 +52,26 @@ def test_noalloc_matches_pcg_solve_on_two_calls(built_lib):
     assert e1 == e2 == 0 and abs(it1 - it2) <= 2 and rel(u2, u1) <= FP64_TOL
 
 
+@pytest.mark.gpu
+def test_noalloc_takes_no_device_memory(built_lib):
+    """The defining claim: after the first call on the device, later calls
+    leave the device's free memory unchanged (nothing is allocated, nothing
+    is cached by the call)."""
+    torch = pytest.importorskip("torch")
+    neq, nelmt, km, ext, dinv, ge = _inputs()
+    u = np.zeros(neq + 1)
+    sg.pcg_solver_noalloc(neq, nelmt, km, u, ext, dinv, ge, 5000, 1e-8)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        u = np.zeros(neq + 1)
+        _, err, _ = sg.pcg_solver_noalloc(neq, nelmt, km, u, ext, dinv, ge, 5000, 1e-8)
+        assert err == 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+
+
 def test_noalloc_rejects_problems_beyond_its_scratch(built_lib):
     """Sizes beyond the 64 MiB static array are refused before any device work."""
     nelmt, neq = 2000, 10
@@ -62,3 +82,19 @@ def test_noalloc_rejects_problems_beyond_its_scratch(built_lib):
         sg.pcg_solver_noalloc(neq, nelmt, k, u, np.zeros(neq + 1), np.zeros(neq + 1), ge, 10, 1e-8)
     assert e.value.code == sg.SG_ERR_BADARG
     assert "64 MiB" in str(e.value)
+
+
+def test_noalloc_rejects_a_dof_map_that_is_not_a_node_numbering(built_lib):
+    """Two slots whose smallest free dof is the same must carry the same three
+    dofs (they are one node); otherwise the call is refused before any device
+    work."""
+    nelmt, neq = 2, 6
+    ge = np.zeros((nelmt, 81), np.int32)
+    ge[0, 0:3] = [1, 2, 3]
+    ge[1, 0:3] = [1, 4, 5]     # same smallest dof 1, different triple
+    u = np.zeros(neq + 1)
+    with pytest.raises(sg.SgError) as e:
+        sg.pcg_solver_noalloc(neq, nelmt, np.zeros((nelmt, 81, 81)), u, np.zeros(neq + 1), np.zeros(neq + 1), ge,
+                              10, 1e-8)
+    assert e.value.code == sg.SG_ERR_BADARG
+    assert "dof triples" in str(e.value)
