@@ -54,6 +54,8 @@ def lib():
         L.orc_principal_stress.argtypes = [i, _dp, _dp, _dp, _dp]
         L.orc_pcg_solver.restype = i
         L.orc_pcg_solver.argtypes = [i, i, _dp, _dp, _dp, _dp, _ip, i, d, C.POINTER(C.c_int)]
+        L.orc_pcg_solver_gpu_order.restype = i
+        L.orc_pcg_solver_gpu_order.argtypes = [i, i, _dp, _dp, _dp, _dp, _ip, i, d, C.POINTER(C.c_int)]
         L.orc_ebe_apply.argtypes = [i, i, _dp, _dp, _ip, _dp]
         L.orc_stress_update.restype = d
         L.orc_stress_update.argtypes = [vp, vp, i, i, _dp, _dp, _dp, _dp, _dp, _dp, d, i, i, _dp, _dp, _dp, vp,
@@ -238,6 +240,18 @@ def pcg_solver(neq, nelmt, k, u, f, dprecon, gdof_elmt, cg_maxiter, cg_tol):
                                np.ascontiguousarray(f, np.float64), np.ascontiguousarray(dprecon, np.float64),
                                np.ascontiguousarray(gdof_elmt, np.int32).reshape(-1), cg_maxiter, cg_tol,
                                C.byref(it))
+    return err, it.value
+
+
+def pcg_solver_gpu_order(neq, nelmt, k, u, f, dprecon, gdof_elmt, cg_maxiter, cg_tol):
+    """pcg_solver evaluated in the GPU drop-in's order (fused multiply-adds,
+    node-by-node gather, grid-shaped dot products); u is updated in place."""
+    it = C.c_int(0)
+    err = lib().orc_pcg_solver_gpu_order(neq, nelmt, np.ascontiguousarray(k, np.float64).reshape(-1), u,
+                                         np.ascontiguousarray(f, np.float64),
+                                         np.ascontiguousarray(dprecon, np.float64),
+                                         np.ascontiguousarray(gdof_elmt, np.int32).reshape(-1), cg_maxiter, cg_tol,
+                                         C.byref(it))
     return err, it.value
 
 

@@ -776,6 +776,182 @@ int pcg_solver(int neq, int nelmt, const double* k, double* u, const double* f,
   return -1;
 }
 
+// pcg_solver (src/solver.f90:14-79) evaluated in the order the GPU drop-in
+// evaluates it, to show that its FP64 kernels differ from the sequential
+// restatement above only by evaluation order.  Same algorithm, same
+// iterates; what changes:
+//  * products are fused multiply-adds, y = fma(K(r,c), p(c), y) for c = 0..80
+//    per element row, u = fma(alpha, p, u), r = fma(-alpha, kp, r),
+//    p = fma(beta, p, z), dot terms s = fma(a, b, s);
+//  * kp(dof) sums its element contributions in element order from zero (the
+//    reference's order) but node by node;
+//  * the dots are grid-shaped: per-thread partials over a grid-stride loop
+//    (r.z over rows 0..neq; p.kp over nodes keyed by their smallest free dof),
+//    a 32-lane xor butterfly per warp, the 8 warps of a block in order, and
+//    the block partials summed by 256 threads in a strided order, then those
+//    256 sums in order.  Grids: rows with ceil(n1/1024) blocks, nodes with
+//    ceil(nodes/512) blocks, each capped at 608 (they depend only on the size).
+// A checker only: it restates the device code's order so that a test can ask
+// for agreement far below the rounding noise of reordering (1e-12, not 1e-8).
+namespace gpuorder {
+constexpr int NT = 256, NW = 8, NPART_CAP = 608;
+int red_grid(long items, long per) {
+  long g = (items + per - 1) / per;
+  return (int)std::max<long>(1, std::min<long>(g, NPART_CAP));
+}
+// xor butterfly of 32 lane values; returns lane 0's result
+double warp_sum(double v[32]) {
+  for (int o = 16; o >= 1; o >>= 1) {
+    double w[32];
+    for (int l = 0; l < 32; ++l) w[l] = v[l] + v[l ^ o];
+    for (int l = 0; l < 32; ++l) v[l] = w[l];
+  }
+  return v[0];
+}
+// block partial from the 256 per-thread partials th[b*256 .. b*256+255]
+double block_sum(const double* th) {
+  double s = 0.0;
+  for (int w = 0; w < NW; ++w) {
+    double v[32];
+    for (int l = 0; l < 32; ++l) v[l] = th[w * 32 + l];
+    s = s + warp_sum(v);
+  }
+  return s;
+}
+// last-block sum of `grid` partials (one quantity per block, stride nq in
+// part, offset q; the thread of index t takes entries t, t+256, ... of the
+// interleaved array of grid*nq values, and only threads with t % nq == q
+// hold quantity q)
+double last_block(const std::vector<double>& part, int grid, int nq, int q) {
+  double sfin[NT];
+  for (int t = 0; t < NT; ++t) {
+    double v = 0.0;
+    for (int idx = t; idx < grid * nq; idx += NT) v = v + part[idx];
+    sfin[t] = v;
+  }
+  double s = 0.0;
+  for (int t = q; t < NT; t += nq) s = s + sfin[t];
+  return s;
+}
+}  // namespace gpuorder
+
+int pcg_solver_gpu_order(int neq, int nelmt, const double* k, double* u, const double* f, const double* dprecon,
+                         const int* gdof_elmt, int cg_maxiter, double cg_tol, int* cg_iter_out) {
+  using namespace gpuorder;
+  const int n1 = neq + 1;
+  const size_t nslots = (size_t)nelmt * NGLL;
+  // nodes keyed by their smallest free dof, in increasing key order; each
+  // lists its element slots in element order
+  std::vector<int> key(nslots), cnt(n1 + 1, 0);
+  for (size_t s = 0; s < nslots; ++s) {
+    const int* g = gdof_elmt + 3 * s;
+    int kk = 0;
+    for (int d = 0; d < 3; ++d)
+      if (g[d] > 0 && (kk == 0 || g[d] < kk)) kk = g[d];
+    key[s] = kk;
+    if (kk) cnt[kk]++;
+  }
+  std::vector<int> gid(n1 + 1, -1);
+  int ng = 0;
+  for (int kk = 1; kk <= neq; ++kk)
+    if (cnt[kk]) gid[kk] = ng++;
+  std::vector<int> gptr(ng + 1, 0), gdof(3 * (size_t)ng, 0);
+  for (int kk = 1; kk <= neq; ++kk)
+    if (cnt[kk]) gptr[gid[kk] + 1] = cnt[kk];
+  for (int g = 0; g < ng; ++g) gptr[g + 1] += gptr[g];
+  std::vector<int> gent(gptr[ng]), fill(gptr.begin(), gptr.end() - 1);
+  for (size_t s = 0; s < nslots; ++s) {
+    if (!key[s]) continue;
+    const int g = gid[key[s]];
+    gent[fill[g]++] = (int)s;
+    for (int d = 0; d < 3; ++d) gdof[3 * (size_t)g + d] = gdof_elmt[3 * s + d];
+  }
+  std::vector<double> Y(nslots * 3), kp(n1, 0.0), p(n1, 0.0), r(n1), z(n1);
+  // element products of p_e = fma(beta, pold_e, z_e) (combine) or of v_e
+  auto apply = [&](const double* v, bool combine, double beta) {
+    for (int e = 0; e < nelmt; ++e) {
+      const int* eg = gdof_elmt + (size_t)e * NEDOF;
+      const double* km = k + (size_t)e * NEDOF * NEDOF;
+      double pe[NEDOF];
+      for (int c = 0; c < NEDOF; ++c) pe[c] = combine ? std::fma(beta, v[eg[c]], z[eg[c]]) : v[eg[c]];
+      for (int rr = 0; rr < NEDOF; ++rr) {
+        double y = 0.0;
+        for (int c = 0; c < NEDOF; ++c) y = std::fma(km[(size_t)c * NEDOF + rr], pe[c], y);
+        Y[(size_t)e * NEDOF + rr] = y;
+      }
+    }
+  };
+  const int ggrid = red_grid(ng, NT * 2), ugrid = red_grid(n1, NT * 4);
+  std::vector<double> th((size_t)std::max(ggrid, ugrid) * NT), part(std::max(ggrid, ugrid) * 4);
+  // gather kp (and, in an iteration, p = fma(beta, p, z) and the p.kp dot)
+  auto gather = [&](bool iter, double beta) -> double {
+    std::fill(th.begin(), th.end(), 0.0);
+    const long wstride = (long)ggrid * NW * 32;
+    for (int g = 0; g < ng; ++g) {
+      const int lane = g % 32;
+      const long W = ((long)(g / 32)) % ((long)ggrid * NW);
+      const long t = W * 32 + lane;  // block W/8, warp W%8
+      (void)wstride;
+      for (int d = 0; d < 3; ++d) {
+        double acc = 0.0;
+        for (int sl = gptr[g]; sl < gptr[g + 1]; ++sl) acc = acc + Y[(size_t)gent[sl] * 3 + d];
+        const int gd = gdof[3 * (size_t)g + d];
+        if (!gd) continue;
+        kp[gd] = acc;
+        if (iter) {
+          p[gd] = std::fma(beta, p[gd], z[gd]);
+          th[t] = std::fma(p[gd], acc, th[t]);
+        }
+      }
+    }
+    if (!iter) return 0.0;
+    for (int b = 0; b < ggrid; ++b) part[b] = block_sum(th.data() + (size_t)b * NT);
+    return last_block(part, ggrid, 1, 0);
+  };
+  // update: u, r, z and the r.z dot (init: r = f - kp, z = D r)
+  double maxp = 0.0, maxu = 0.0;
+  auto update = [&](bool init, double alpha) -> double {
+    std::fill(th.begin(), th.end(), 0.0);
+    const long S = (long)ugrid * NT;
+    maxp = 0.0; maxu = 0.0;
+    for (long i = 0; i < n1; ++i) {
+      const long t = i % S;
+      if (init) {
+        r[i] = f[i] - kp[i];
+        z[i] = dprecon[i] * r[i];
+      } else {
+        u[i] = std::fma(alpha, p[i], u[i]);
+        r[i] = std::fma(-alpha, kp[i], r[i]);
+        z[i] = dprecon[i] * r[i];
+        maxp = std::max(maxp, std::fabs(p[i]));
+        maxu = std::max(maxu, std::fabs(u[i]));
+      }
+      th[t] = std::fma(r[i], z[i], th[t]);
+    }
+    for (int b = 0; b < ugrid; ++b) {
+      part[(size_t)b * 4 + 0] = part[(size_t)b * 4 + 1] = part[(size_t)b * 4 + 3] = 0.0;
+      part[(size_t)b * 4 + 2] = block_sum(th.data() + (size_t)b * NT);
+    }
+    return last_block(part, ugrid, 4, 2);
+  };
+  apply(u, false, 0.0);
+  gather(false, 0.0);
+  double rz = update(true, 0.0), beta = 0.0;
+  for (int it = 1; it <= cg_maxiter; ++it) {
+    apply(p.data(), true, beta);
+    const double alpha = rz / gather(true, beta);
+    const double s = update(false, alpha);
+    if (std::fabs(alpha) * maxp / maxu <= cg_tol) {
+      *cg_iter_out = it;
+      return 0;
+    }
+    beta = s / rz;
+    rz = s;
+  }
+  *cg_iter_out = cg_maxiter + 1;
+  return -1;
+}
+
 // One pass of the per-element / per-GLL-point stress, yield, flow and body-load
 // block inlined in slope3d (src/slope.F90:311-383) and excavation3d
 // (src/excavation.F90:546-616).  `finalize` = (nl_isconv .or. nl_iter==nl_maxiter).
@@ -1326,6 +1502,13 @@ void orc_set_eqload(void* hv, double eqkx, double eqky, double eqkz) {
 int orc_pcg_solver(int neq, int nelmt, const double* k, double* u, const double* f, const double* dprecon,
                    const int* gdof_elmt, int cg_maxiter, double cg_tol, int* cg_iter) {
   return pcg_solver(neq, nelmt, k, u, f, dprecon, gdof_elmt, cg_maxiter, cg_tol, cg_iter);
+}
+
+// pcg_solver in the GPU drop-in's evaluation order (a checker of the device
+// kernels' arithmetic, see pcg_solver_gpu_order)
+int orc_pcg_solver_gpu_order(int neq, int nelmt, const double* k, double* u, const double* f, const double* dprecon,
+                             const int* gdof_elmt, int cg_maxiter, double cg_tol, int* cg_iter) {
+  return pcg_solver_gpu_order(neq, nelmt, k, u, f, dprecon, gdof_elmt, cg_maxiter, cg_tol, cg_iter);
 }
 
 void orc_ebe_apply(int neq, int nelmt, const double* k, const double* p, const int* gdof_elmt, double* kp) {

@@ -1,0 +1,143 @@
+"""GPU parity on the layered 3D slope class of the 192k-element benchmark.
+
+The benchmark mesh (3D, 1:2 slope face, three layers, every element its own
+lognormally perturbed material block, so that dt_viscoplas is a minimum over
+thousands of blocks) is cut to 24 x 4 x 6 = 576 elements, small enough for the
+serial oracle.  Checked here, each against the oracle:
+
+* the FP64 drop-in (sg_pcg_solve) against the oracle's pcg_solver evaluated
+  in the GPU's order (fused multiply-adds, node-by-node gather, grid-shaped
+  dot products): <= 1e-12, which shows that the FP64 kernels are exact up to
+  evaluation order; and against the sequential pcg_solver: <= 1e-9 relative
+  L2 (the 1e-9 target for the FP64 path), and <= 1e-9 on the 300-element
+  slope once the step tolerance is tight enough that the stopping iteration
+  no longer carries the rounding of the summation order;
+* FP64 plastic trials of the device model (sparse FP64 element apply) at
+  SRF 1.0 and 1.3 (48 and 217 plastic iterations in the oracle);
+* the mixed FP32/FP64 form with the stored-matrix lane apply -- the default
+  apply of the benchmark's 192k mesh, forced here on the small cut with
+  SG_APPLY_VARIANT=3 -- and with the default operator of this size
+  (matrix-free), each in an 8-trial batch: displacements within 1e-6 of the
+  FP64 oracle and the same plastic-iteration counts.
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+import specfem3d_geotech_gb300 as sg
+from oracle.pyoracle import OracleModel, pcg_solver as orc_pcg, pcg_solver_gpu_order as orc_pcg_gpu
+from oracle_jobs import SLOPE3D_CUT, slope3d_cut, slope3d_cut_trials
+from specfem3d_geotech_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+MATCHED_ORDER_TOL = 1e-12   # GPU vs the oracle in the GPU's evaluation order
+FP64_TARGET = 1e-9          # the FP64 path's displacement target vs the sequential oracle
+TRIAL_TOL = 5e-8            # a whole FP64 trial (the reordering noise floor of a trial is 4e-8)
+STRESS_TOL = 2e-5
+FMAX_TOL = 2e-3
+MIXED_TOL = 1e-6            # mixed FP32/FP64 form vs the FP64 oracle
+SRFS = (1.0, 1.3)
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def cut():
+    mesh = slope3d_cut()
+    return mesh, OracleModel(mesh)
+
+
+@pytest.fixture(scope="module")
+def oracle_trials():
+    return slope3d_cut_trials(list(SRFS))
+
+
+def _dropin_inputs(om):
+    km, dp, ext = om.stiffness_bodyload()
+    dinv = np.where(np.arange(om.neq + 1) > 0, 1.0 / np.where(dp == 0, 1, dp), 0.0)
+    return km, dinv, ext, om.arrays()["gdof_elmt"]
+
+
+@pytest.mark.parametrize("name", ["slope3d_cut", "slope2d"])
+def test_dropin_fp64_exact_up_to_evaluation_order(ctx, cut, name):
+    om = cut[1] if name == "slope3d_cut" else OracleModel(meshgen.slope2d())
+    km, dinv, ext, ge = _dropin_inputs(om)
+    for tol in (1e-8, 1e-12):
+        u_ref = np.zeros(om.neq + 1)
+        err_r, it_r = orc_pcg_gpu(om.neq, om.nelmt, km, u_ref, ext, dinv, ge, 20000, tol)
+        u = np.zeros(om.neq + 1)
+        it, err, _ = sg.pcg_solver(om.neq, om.nelmt, km, u, ext, dinv, ge, 20000, tol, ctx=ctx)
+        assert err == err_r == 0
+        assert it == it_r
+        assert rel(u, u_ref) <= MATCHED_ORDER_TOL, rel(u, u_ref)
+
+
+def test_dropin_fp64_within_1e9_of_sequential_oracle(ctx, cut):
+    # the 3D cut at the reference's step tolerance
+    om = cut[1]
+    km, dinv, ext, ge = _dropin_inputs(om)
+    u_ref = np.zeros(om.neq + 1)
+    err_r, it_r = orc_pcg(om.neq, om.nelmt, km, u_ref, ext, dinv, ge, 5000, 1e-8)
+    u = np.zeros(om.neq + 1)
+    it, err, _ = sg.pcg_solver(om.neq, om.nelmt, km, u, ext, dinv, ge, 5000, 1e-8, ctx=ctx)
+    assert err == err_r == 0 and abs(it - it_r) <= 2
+    assert rel(u, u_ref) <= FP64_TARGET, rel(u, u_ref)
+    # the 300-element slope stops at cg_tol = 1e-8 with 2e-9 of summation-order
+    # rounding in the last step; with a tight step tolerance both reach 1e-9
+    om2 = OracleModel(meshgen.slope2d())
+    km, dinv, ext, ge = _dropin_inputs(om2)
+    u_ref = np.zeros(om2.neq + 1)
+    orc_pcg(om2.neq, om2.nelmt, km, u_ref, ext, dinv, ge, 20000, 1e-12)
+    u = np.zeros(om2.neq + 1)
+    _, err, _ = sg.pcg_solver(om2.neq, om2.nelmt, km, u, ext, dinv, ge, 20000, 1e-12, ctx=ctx)
+    assert err == 0 and rel(u, u_ref) <= FP64_TARGET, rel(u, u_ref)
+
+
+def test_fp64_trials_match_oracle(ctx, cut, oracle_trials):
+    mesh, om = cut
+    m = sg.Model(mesh, ctx=ctx)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=2000)
+    for t, srf in enumerate(SRFS):
+        (r,), x = m.trials([srf], ctl, want_x=True)
+        ro = oracle_trials[srf]
+        assert r["nl_iter"] == ro["nl_iter"] and r["converged"] == ro["converged"] == 1, (srf, r, ro)
+        assert abs(r["cg_tot"] - ro["cg_tot"]) <= max(3, 0.01 * ro["cg_tot"])
+        assert rel(x[0], ro["x"]) <= TRIAL_TOL, rel(x[0], ro["x"])
+        st = m.last_stress(0)
+        assert np.abs(st - ro["stress"]).max() <= STRESS_TOL * np.abs(ro["stress"]).max()
+        assert abs(r["umax"] - ro["umax"]) <= TRIAL_TOL * abs(ro["umax"])
+        assert abs(r["fmax"] - ro["fmax"]) <= FMAX_TOL * abs(ro["fmax"])
+
+
+def _mixed_batch(variant, out):
+    """An 8-trial mixed batch on the 3D cut in a fresh process (the apply
+    variant is read when the context is created)."""
+    srfs = list(SRFS) + [1.05, 1.1, 1.15, 1.2, 1.25, 1.35]
+    code = ("import sys; sys.path.insert(0, %r); import numpy as np; import specfem3d_geotech_gb300 as sg;"
+            "from specfem3d_geotech_gb300 import meshgen; m = sg.Model(meshgen.slope3d(**%r), precision=sg.PREC_MIXED);"
+            "r, x = m.trials(%r, sg.make_control(precision=sg.PREC_MIXED), want_x=True);"
+            "np.savez(%r, x=x, nl=np.array([t['nl_iter'] for t in r]), conv=np.array([t['converged'] for t in r]),"
+            "stress=np.stack([m.last_stress(t) for t in range(2)]))") % (ROOT, SLOPE3D_CUT, srfs, str(out))
+    env = dict(os.environ)
+    if variant is not None:
+        env["SG_APPLY_VARIANT"] = str(variant)
+    subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=900)
+    return np.load(out)
+
+
+@pytest.mark.parametrize("variant", [3, None], ids=["lane_apply", "default"])
+def test_mixed_batched_trials_match_fp64_oracle(tmp_path, oracle_trials, variant):
+    d = _mixed_batch(variant, tmp_path / "mixed.npz")
+    for t, srf in enumerate(SRFS):
+        ro = oracle_trials[srf]
+        assert int(d["nl"][t]) == ro["nl_iter"] and int(d["conv"][t]) == 1, (srf, d["nl"][t], ro["nl_iter"])
+        assert rel(d["x"][t], ro["x"]) <= MIXED_TOL, (srf, rel(d["x"][t], ro["x"]))
+        smax = np.abs(ro["stress"]).max()
+        assert np.abs(d["stress"][t] - ro["stress"]).max() <= STRESS_TOL * smax
