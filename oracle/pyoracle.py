@@ -67,6 +67,8 @@ def lib():
         L.orc_dt_viscoplas.restype = d
         L.orc_dt_viscoplas.argtypes = [i, _dp, _dp, _dp]
         L.orc_slope_trial.argtypes = [vp, d, _dp, vp, vp, vp]
+        L.orc_last_uerr_log.restype = i
+        L.orc_last_uerr_log.argtypes = [vp, vp]
         L.orc_slope_sweep.restype = i
         L.orc_slope_sweep.argtypes = [vp, i, _dp, _dp]
         L.orc_fos_bisection.restype = d
@@ -204,6 +206,10 @@ class OracleModel:
             out["stress"] = st.reshape(self.nelmt, 27, 6)
         if want_log:
             out["nl_cg"] = nl[: out["nl_iter"]]
+            n = lib().orc_last_uerr_log(self.h, None)
+            ue = np.zeros(max(n, 1))
+            lib().orc_last_uerr_log(self.h, ue.ctypes.data)
+            out["uerr_log"] = ue[:n]
         return out
 
     def sweep(self, srf):

@@ -1118,6 +1118,7 @@ struct TrialResult {
 struct SlopeState {
   std::vector<double> storekm, dprecon, extload, bodyload, load, x, oldx, evpt, stress;
   std::vector<int> nl_cg_log;  // cg iterations per NL iteration of the last trial
+  std::vector<double> uerr_log;  // uerr per NL iteration of the last trial
 };
 
 struct Control {
@@ -1160,6 +1161,7 @@ TrialResult slope_trial(const Model& M, const Control& C, SlopeState& S, double 
   S.oldx.assign(n1, 0.0);
   S.load.assign(n1, 0.0);
   S.nl_cg_log.clear();
+  S.uerr_log.clear();
   int nl_iter = 1;
   bool nl_isconv = false;
   double fmax = 0, uerr = 0;
@@ -1171,6 +1173,7 @@ TrialResult slope_trial(const Model& M, const Control& C, SlopeState& S, double 
     int err = pcg_solver(M.neq, M.nelmt, S.storekm.data(), S.x.data(), S.load.data(), S.dprecon.data(),
                          M.gdof_elmt.data(), C.cg_maxiter, C.cg_tol, &cg_iter);
     S.nl_cg_log.push_back(cg_iter);
+    S.uerr_log.push_back(0.0);
     if (err != 0) { R.errcode = err; R.nl_iter = nl_iter; return R; }
     R.cg_tot += cg_iter;
     S.x[0] = 0.0;
@@ -1181,6 +1184,7 @@ TrialResult slope_trial(const Model& M, const Control& C, SlopeState& S, double 
     double num = 0.0, den = 0.0;
     for (int i = 0; i < n1; ++i) { num = std::max(num, std::fabs(S.x[i] - S.oldx[i])); den = std::max(den, std::fabs(S.x[i])); }
     uerr = num / den;
+    S.uerr_log.back() = uerr;
     S.oldx = S.x;
     nl_isconv = uerr <= C.nl_tol;
     bool finalize = nl_isconv || nl_iter == C.nl_maxiter;
@@ -1564,6 +1568,14 @@ void orc_slope_trial(void* hv, double srf, double* res, double* x_out, double* s
   if (x_out) std::memcpy(x_out, h->S.x.data(), sizeof(double) * h->S.x.size());
   if (stress_out) std::memcpy(stress_out, h->S.stress.data(), sizeof(double) * h->S.stress.size());
   if (nl_cg) for (size_t i = 0; i < h->S.nl_cg_log.size(); ++i) nl_cg[i] = h->S.nl_cg_log[i];
+}
+
+// uerr of every plastic iteration of the last trial (the convergence margin of
+// src/slope.F90:307-310); returns the number of entries
+int orc_last_uerr_log(void* hv, double* out) {
+  OrcModel* h = (OrcModel*)hv;
+  if (out) std::memcpy(out, h->S.uerr_log.data(), sizeof(double) * h->S.uerr_log.size());
+  return (int)h->S.uerr_log.size();
 }
 
 // The slope3d SRF sweep: runs srf[0..nsrf) in order and stops after the first

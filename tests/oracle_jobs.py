@@ -26,7 +26,7 @@ def slope3d_cut():
 def _trial(srf: float):
     from oracle.pyoracle import OracleModel
     om = OracleModel(slope3d_cut())
-    r = om.trial(srf, want_x=True, want_stress=True)
+    r = om.trial(srf, want_x=True, want_stress=True, want_log=True)
     return {k: (np.asarray(v) if isinstance(v, np.ndarray) else v) for k, v in r.items()}
 
 

@@ -13,7 +13,7 @@ serial oracle.  Checked here, each against the oracle:
   slope once the step tolerance is tight enough that the stopping iteration
   no longer carries the rounding of the summation order;
 * FP64 plastic trials of the device model (sparse FP64 element apply) at
-  SRF 1.0 and 1.3 (48 and 217 plastic iterations in the oracle);
+  SRF 1.0 and 1.2 (48 and 107 plastic iterations in the oracle);
 * the mixed FP32/FP64 form with the stored-matrix lane apply -- the default
   apply of the benchmark's 192k mesh, forced here on the small cut with
   SG_APPLY_VARIANT=3 -- and with the default operator of this size
@@ -40,7 +40,13 @@ TRIAL_TOL = 5e-8            # a whole FP64 trial (the reordering noise floor of 
 STRESS_TOL = 2e-5
 FMAX_TOL = 2e-3
 MIXED_TOL = 1e-6            # mixed FP32/FP64 form vs the FP64 oracle
-SRFS = (1.0, 1.3)
+# Trials whose plastic-iteration count is not a rounding decision: the
+# oracle's uerr at the last iteration is at least 0.5 % below nl_tol and at the
+# one before at least 0.5 % above it.  (At SRF 1.3 the last uerr sits 0.19 %
+# below nl_tol, and the GPU, whose displacements differ from the oracle's by
+# reordering noise of ~1e-8, stops one plastic iteration later.)
+SRFS = (1.0, 1.2)
+MARGIN = 5e-3
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -56,7 +62,11 @@ def cut():
 
 @pytest.fixture(scope="module")
 def oracle_trials():
-    return slope3d_cut_trials(list(SRFS))
+    res = slope3d_cut_trials(list(SRFS))
+    for srf, r in res.items():
+        ue = r["uerr_log"]
+        assert (1e-4 - ue[-1]) >= MARGIN * 1e-4 and (ue[-2] - 1e-4) >= MARGIN * 1e-4, (srf, ue[-2:])
+    return res
 
 
 def _dropin_inputs(om):
@@ -119,7 +129,7 @@ def test_fp64_trials_match_oracle(ctx, cut, oracle_trials):
 def _mixed_batch(variant, out):
     """An 8-trial mixed batch on the 3D cut in a fresh process (the apply
     variant is read when the context is created)."""
-    srfs = list(SRFS) + [1.05, 1.1, 1.15, 1.2, 1.25, 1.35]
+    srfs = list(SRFS) + [1.05, 1.1, 1.15, 1.25, 1.3, 1.35]
     code = ("import sys; sys.path.insert(0, %r); import numpy as np; import specfem3d_geotech_gb300 as sg;"
             "from specfem3d_geotech_gb300 import meshgen; m = sg.Model(meshgen.slope3d(**%r), precision=sg.PREC_MIXED);"
             "r, x = m.trials(%r, sg.make_control(precision=sg.PREC_MIXED), want_x=True);"
