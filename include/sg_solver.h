@@ -279,8 +279,13 @@ int sg_srf_sweep(sg_model* model, const sg_control* ctl, int nsrf, const double*
 
 /* Critical SRF on the grid lo + step*m (m = 0..round((hi-lo)/step)), the
  * smallest grid SRF whose trial fails, assuming lo is stable and hi fails.
- * k = 1 is plain bisection; k > 1 probes k grid points per round (k-section)
- * as one batched trial set.  *ntrials and *nrounds report the work done. */
+ * k = 1 is plain bisection.  k > 1 keeps k trials running as one batch and
+ * refills it as results arrive: a converged trial raises the stable bound, a
+ * failed one lowers the failing bound, trials outside the bracket are
+ * cancelled and free slots take the midpoints of the widest open gaps.  The
+ * answer is the bisection's when failure is monotone in SRF.  *ntrials =
+ * trials started; *nrounds = bisection steps (k = 1) or result events waited
+ * for (k > 1). */
 int sg_fos(sg_model* model, const sg_control* ctl, double lo, double hi, double step, int k,
            double* fos, int* ntrials, int* nrounds);
 

@@ -1466,39 +1466,113 @@ int sg_srf_sweep(sg_model* M, const sg_control* ctl, int nsrf, const double* srf
   return st;
 }
 
-// Critical SRF on a grid by k-section: each round probes k grid points spread
-// evenly inside the current bracket (a, b) as one batched trial set, then
-// keeps the sub-interval between the last stable and the first failed probe.
+// Critical SRF on the grid lo + step*m, m = 0..Mg: the smallest grid SRF whose
+// trial fails (the failure test of src/slope.F90:441, nl_iter == nl_maxiter),
+// assuming lo is stable and hi fails, as a bisection does.
+//
+// k = 1: bisection, one trial at a time.
+// k > 1: a continuously refilled batch of k trials.  A trial that converges
+// raises the stable bound a, one that fails lowers the failing bound b, and
+// every running trial outside (a, b) is cancelled; each free slot takes the
+// midpoint of the widest open gap between a, the running probes and b (gaps
+// above the lowest running probe count half: they matter only if that probe
+// converges).  Converging trials report after tens to hundreds of plastic
+// iterations while failing ones take nl_maxiter, so the bracket closes from
+// below while the failures are still running, and the search needs about
+// two failure waits instead of one per k-section round.  Under the same
+// monotonicity the answer is the bisection's.
+// *ntrials = trials started, *nrounds = result events the search waited for.
+static int fos_batched(sg_model* M, const sg_control* ctl, double lo, double step, int Mg, int k, int* b_out,
+                       int* ntrials, int* nrounds) {
+  int st = batch_begin_impl(M, ctl, k);
+  if (st != SG_OK) return st;
+  Batch& B = M->B;
+  int a = 0, b = Mg, nt = 0, nr = 0;
+  std::vector<int> idx(k, -1);   // grid index of each slot's trial, -1 free
+  while (true) {
+    // fill the free slots
+    for (int j = 0; j < k; ++j) {
+      if (idx[j] >= 0) continue;
+      std::vector<int> S = {a, b};
+      int low = b;
+      for (int t = 0; t < k; ++t)
+        if (idx[t] >= 0) { S.push_back(idx[t]); low = std::min(low, idx[t]); }
+      std::sort(S.begin(), S.end());
+      double best = -1.0;
+      int pick = -1;
+      for (size_t q = 0; q + 1 < S.size(); ++q) {
+        const int g = S[q + 1] - S[q];
+        if (g < 2) continue;
+        const double w = g * (S[q + 1] <= low ? 1.0 : 0.5);
+        if (w > best) { best = w; pick = S[q] + g / 2; }
+      }
+      if (pick < 0) break;
+      int slot = -1;
+      st = batch_add_impl(M, lo + step * pick, &slot);
+      if (st != SG_OK) { batch_end_impl(M); return st; }
+      idx[slot] = pick;
+      ++nt;
+    }
+    bool any = false;
+    for (int j = 0; j < k; ++j) any = any || idx[j] >= 0;
+    if (!any) break;
+    // plastic iterations until at least one trial has finished
+    bool done = false;
+    while (!done) {
+      st = batch_iteration(M);
+      if (st != SG_OK) { batch_end_impl(M); return st; }
+      for (int j = 0; j < k; ++j) done = done || (idx[j] >= 0 && !B.slot[j].live);
+    }
+    ++nr;
+    for (int j = 0; j < k; ++j) {
+      if (idx[j] < 0 || B.slot[j].live) continue;
+      const sg_trial_result& r = B.slot[j].res;
+      if (r.errcode != SG_OK) { batch_end_impl(M); return r.errcode; }
+      if (r.failed) b = std::min(b, idx[j]);
+      else a = std::max(a, idx[j]);
+      B.slot[j] = Slot();
+      idx[j] = -1;
+    }
+    // cancel the trials that can no longer move the bracket
+    for (int j = 0; j < k; ++j)
+      if (idx[j] >= 0 && (idx[j] <= a || idx[j] >= b)) {
+        B.slot[j] = Slot();
+        idx[j] = -1;
+      }
+    if (b - a <= 1) break;
+  }
+  batch_end_impl(M);
+  *b_out = b;
+  if (ntrials) *ntrials = nt;
+  if (nrounds) *nrounds = nr;
+  return SG_OK;
+}
+
 int sg_fos(sg_model* M, const sg_control* ctl, double lo, double hi, double step, int k, double* fos, int* ntrials,
            int* nrounds) {
   if (!M || !ctl || step <= 0 || hi <= lo || k < 1 || k > 16 || !fos) return SG_ERR_BADARG;
-  int Mg = (int)std::lround((hi - lo) / step);
-  int a = 0, b = Mg, nt = 0, nr = 0;
-  while (b - a > 1) {
-    int gap = b - a - 1;
-    int kk = std::min(k, gap);
-    std::vector<int> probe(kk);
-    for (int t = 0; t < kk; ++t) probe[t] = a + (int)(((long long)(t + 1) * (b - a)) / (kk + 1));
-    probe.erase(std::unique(probe.begin(), probe.end()), probe.end());
-    kk = (int)probe.size();
-    std::vector<double> srf(kk);
-    for (int t = 0; t < kk; ++t) srf[t] = lo + step * probe[t];
-    std::vector<sg_trial_result> res(kk);
-    int st = run_trials(M, ctl, kk, srf.data(), res.data(), nullptr);
-    nt += kk;
-    ++nr;
+  const int Mg = (int)std::lround((hi - lo) / step);
+  if (k > 1) {
+    int b = Mg;
+    int st = fos_batched(M, ctl, lo, step, Mg, k, &b, ntrials, nrounds);
     if (st != SG_OK) return st;
-    int na = a, nb = b;
-    for (int t = 0; t < kk; ++t) {
-      if (res[t].failed) { nb = probe[t]; break; }
-      na = probe[t];
-    }
-    a = na;
-    b = nb;
+    *fos = lo + step * b;
+    return SG_OK;
+  }
+  int a = 0, b = Mg, nt = 0;
+  while (b - a > 1) {
+    const int m = (a + b) / 2;
+    const double srf = lo + step * m;
+    sg_trial_result res;
+    int st = run_trials(M, ctl, 1, &srf, &res, nullptr);
+    ++nt;
+    if (st != SG_OK) return st;
+    if (res.failed) b = m;
+    else a = m;
   }
   *fos = lo + step * b;
   if (ntrials) *ntrials = nt;
-  if (nrounds) *nrounds = nr;
+  if (nrounds) *nrounds = nt;
   return SG_OK;
 }
 

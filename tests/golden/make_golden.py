@@ -6,6 +6,7 @@ small JSON files instead of being recomputed in every test session.
 
     python tests/golden/make_golden.py slope2d_sweep     # ~20-40 min, 1 core
     python tests/golden/make_golden.py slope2d_trials    # ~1 min
+    python tests/golden/make_golden.py slope3d_cut_fos   # ~1 h, 1 core
 """
 from __future__ import annotations
 
@@ -53,6 +54,38 @@ def slope2d_trials():
         rows.append(r)
     with open(os.path.join(HERE, "slope2d_trials.json"), "w") as f:
         json.dump(dict(mesh="slope2d", trials=rows), f, indent=1)
+
+
+def slope3d_cut_fos():
+    """Critical SRF of the 576-element cut of the layered 3D slope (the mesh of
+    tests/test_gpu_config1.py) by the oracle's bisection on [1, 3] to 0.01 --
+    the same probes as orc_fos_bisection -- with every probe's summary, so
+    that the GPU's factor-of-safety searches and the near-critical trials of
+    the precision report can be checked against it without an hour of CPU."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_jobs import SLOPE3D_CUT, slope3d_cut
+    om = OracleModel(slope3d_cut())
+    t0 = time.time()
+    lo, hi, step = 1.0, 3.0, 0.01
+    a, b = 0, int(round((hi - lo) / step))
+    rows = []
+    while b - a > 1:
+        m = (a + b) // 2
+        r = om.trial(lo + step * m, want_log=True)
+        ue = r.pop("uerr_log")
+        r.pop("nl_cg")
+        r["uerr_last2"] = [float(v) for v in ue[-2:]]
+        r["seconds"] = time.time() - t0
+        rows.append(r)
+        print(json.dumps(r), flush=True)
+        if r["failed"]:
+            b = m
+        else:
+            a = m
+    out = dict(mesh="slope3d", cut=SLOPE3D_CUT, nelmt=om.nelmt, neq=om.neq, search="bisection on [1, 3] step 0.01",
+               critical_srf=round(lo + step * b, 10), probes=rows, oracle_seconds=time.time() - t0)
+    with open(os.path.join(HERE, "slope3d_cut_fos.json"), "w") as f:
+        json.dump(out, f, indent=1)
 
 
 if __name__ == "__main__":
