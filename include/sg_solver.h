@@ -288,6 +288,11 @@ int sg_srf_sweep(sg_model* model, const sg_control* ctl, int nsrf, const double*
  * for (k > 1). */
 int sg_fos(sg_model* model, const sg_control* ctl, double lo, double hi, double step, int k,
            double* fos, int* ntrials, int* nrounds);
+/* Plastic iterations run by the model's last sg_fos: batch iterations for
+ * k > 1 (one iteration of all the batch's trials counts once), trial
+ * iterations summed over the bisection's trials for k = 1.  No counterpart in
+ * the reference (its SRF loop prints per-trial counts only). */
+int sg_fos_steps(const sg_model* model, long long* steps);
 
 /* ---- request loop: factor-of-safety and excavation solves of many meshes --
  * Requests are queued on submission and admitted in arrival order when their

@@ -38,7 +38,7 @@ EXPORTED = (
     "sg_model_control", "sg_model_stiffness", "sg_model_set_eqload", "sg_model_set_water", "sg_model_set_pore_pressure",
     "sg_model_pore_pressure", "sg_nodal_stress", "sg_excavation_fields",
     "sg_principal_stress", "sg_write_summary_header", "sg_write_summary_row", "sg_write_ensight_case", "sg_write_ensight_geo",
-    "sg_write_ensight_var", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos",
+    "sg_write_ensight_var", "sg_srf_trials", "sg_last_stress", "sg_srf_sweep", "sg_fos", "sg_fos_steps",
     "sg_excavation", "sg_profile_enable", "sg_profile_read", "sg_batch_begin", "sg_batch_add", "sg_batch_step",
     "sg_batch_poll", "sg_batch_release", "sg_batch_end", "sg_timer_mark", "sg_timer_ms", "sg_pcg_solve_noalloc", "sg_stress_bodyload", "sg_mesh_from_deck", "sg_mesh_free", "sg_mesh_info",
     "sg_mesh_arrays", "sg_mesh_control",
@@ -166,6 +166,8 @@ def lib(path: Optional[str] = None):
     L.sg_fos.restype = i
     L.sg_fos.argtypes = [vp, C.POINTER(Control), d, d, d, i, C.POINTER(C.c_double), C.POINTER(C.c_int),
                          C.POINTER(C.c_int)]
+    L.sg_fos_steps.restype = i
+    L.sg_fos_steps.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.sg_excavation.restype = i
     L.sg_excavation.argtypes = [vp, C.POINTER(Control), i, d, d, d, i, vp, vp, i, d, vp, C.POINTER(C.c_int)]
     L.sg_profile_enable.restype = i
@@ -555,6 +557,15 @@ class Model:
         if st:
             raise SgError(st, self.ctx.last_error)
         return v.value, nt.value, nr.value
+
+    def fos_steps(self) -> int:
+        """Plastic iterations of the last fos(): batch iterations for k > 1,
+        trial iterations summed over the bisection's trials for k = 1."""
+        n = C.c_longlong(0)
+        st = lib().sg_fos_steps(self.h, C.byref(n))
+        if st:
+            raise SgError(st, "sg_fos_steps")
+        return int(n.value)
 
     # ---- continuous batching -------------------------------------------
     def batch_begin(self, ctl: Control, kmax: int):

@@ -621,6 +621,8 @@ struct sg_model {
   std::vector<double> ex_vmeps, ex_scf;  // nodal fields of the last excavation stage
   double* d_fpart = nullptr;
   double* d_wp = nullptr;  // pore pressure per node (water table set), else null
+  long long plastic_steps = 0;  // batch plastic iterations run (all trials of a batch step count once)
+  long long fos_steps = 0;      // of them, by the last sg_fos
 };
 
 static void model_release_work(sg_model* M) {
@@ -1238,6 +1240,7 @@ static void slot_finish(sg_model* M, int j) {
 // One plastic iteration (src/slope.F90:285-391) of every live slot.
 static int batch_iteration(sg_model* M) {
   sg_ctx* c = M->ctx;
+  M->plastic_steps++;
   HostMesh& h = M->H;
   Batch& B = M->B;
   TrialWork& W = M->W;
@@ -1552,9 +1555,11 @@ int sg_fos(sg_model* M, const sg_control* ctl, double lo, double hi, double step
            int* nrounds) {
   if (!M || !ctl || step <= 0 || hi <= lo || k < 1 || k > 16 || !fos) return SG_ERR_BADARG;
   const int Mg = (int)std::lround((hi - lo) / step);
+  const long long steps0 = M->plastic_steps;
   if (k > 1) {
     int b = Mg;
     int st = fos_batched(M, ctl, lo, step, Mg, k, &b, ntrials, nrounds);
+    M->fos_steps = M->plastic_steps - steps0;
     if (st != SG_OK) return st;
     *fos = lo + step * b;
     return SG_OK;
@@ -1573,6 +1578,13 @@ int sg_fos(sg_model* M, const sg_control* ctl, double lo, double hi, double step
   *fos = lo + step * b;
   if (ntrials) *ntrials = nt;
   if (nrounds) *nrounds = nt;
+  M->fos_steps = M->plastic_steps - steps0;
+  return SG_OK;
+}
+
+int sg_fos_steps(const sg_model* M, long long* steps) {
+  if (!M || !steps) return SG_ERR_BADARG;
+  *steps = M->fos_steps;
   return SG_OK;
 }
 
