@@ -3,19 +3,23 @@
 
 Workload (the 3D slope the headline metric is quoted on): 120x40x40 mapped
 hex mesh, NGLL=3, 4.63M dofs, three lognormally perturbed layers, seeded
-synthetic data.  Form measured: the mixed-precision batched serving form --
+synthetic data; a factor-of-safety solve searches SRF on [1, 3] to 0.01 with
+nl_maxiter = 2000.  Form measured: the mixed-precision batched serving form --
 FP32 element matrices and FP32 PCG with FP64 iterative refinement, k = 8
-concurrent SRF trials sharing every element apply as 8 right-hand sides.
+concurrent SRF trials sharing every element apply as 8 right-hand sides, the
+batch refilled as trials finish (sg_fos with k = 8).
 
 A step is one pass of the hot path over one batch: one plastic iteration of
-all 8 trials (FP64-refined linear solve to the reference tolerances, then the
-stress / yield / body-load update of each trial).  A full FOS solve on this
-mesh runs for hours (failing trials run nl_maxiter = 2000 plastic iterations
-of ~825 PCG iterations each), so FOS solves/s is derived from the measured
-trial-plastic-iteration rate with a fixed work model: one FOS solve = 8
-bisection trials x 2000 plastic iterations (an upper bound on the work, so
-the figure is a lower bound on throughput).  Both arms use the same model,
-so their ratio is the ratio of measured rates.
+the 8 trials (FP64-refined linear solve to the reference tolerances, then the
+stress / yield / body-load update of each trial).  A whole FOS solve on the
+192k mesh runs for hours, so FOS solves/s = 1 / (plastic iterations per FOS
+solve x seconds per plastic iteration): the seconds are measured on the 192k
+mesh, the iteration count is measured in the same run by a complete search of
+the same slope cut to 24 x 4 x 6 = 576 elements (the fos_measured leg), where
+the search also runs to the end and is timed as is.  The plain FP64 line and
+the CPU reference use the same counts for their own search (bisection, one
+trial at a time): the GPU's plain bisection on the cut, and the oracle's
+bisection on the cut (tests/golden/slope3d_cut_fos.json).
 
 Arms: default (ours, CUDA library through the C ABI) or --impl reference
 (the CPU oracle -- a restatement of the reference's serial Fortran path --
@@ -35,15 +39,50 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 METRIC = "FOS solves/sec + p50/p99 latency, mixed-prec batched vs plain FP64 GPU"
 UNIT = "FOS solves/s"
 NL_MAXITER = 2000
-FOS_TRIALS = 8               # bisection trials per FOS solve on [1,3] to 0.01
-FOS_WORK = FOS_TRIALS * NL_MAXITER   # trial plastic iterations per FOS solve (upper bound)
-N_CG_REF = 825               # PCG iterations per plastic iteration of the FP64 reference algorithm on this mesh
+SRF_LO, SRF_HI, SRF_STEP = 1.0, 3.0, 0.01
+GRID = int(round((SRF_HI - SRF_LO) / SRF_STEP))
+BISECT_TRIALS = math.ceil(math.log2(GRID))   # 8 trials of a bisection on the 200-step grid
+# FP64 PCG iterations per plastic iteration of the reference algorithm on the
+# 192k mesh (the plain FP64 leg of this benchmark measures 802.9 at the
+# benchmark's SRF); both arms scale the CPU sample with this one number.
+N_CG_REF = 803
 K_TRIALS = 8
 CPU_SAMPLE_ITERS = 200       # PCG iterations of the oracle's timed sample (about 10 s of CPU work)
+CUT = dict(nx=24, ny=4, nz=6)   # the 576-element cut of the benchmark slope
+GOLDEN_FOS = os.path.join(ROOT, "tests", "golden", "slope3d_cut_fos.json")
+
+
+def workload_config(world: int, ne: int = 192000, neq: int = 4633520, nx: int = 120) -> dict:
+    """The config object both arms print (one workload, one work model)."""
+    return {"workload": f"slope3d_{ne // 1000}k factor-of-safety solve ({nx}x40x40 hex, NGLL=3, {neq} dof; "
+                        f"SRF on [{SRF_LO:g}, {SRF_HI:g}] to {SRF_STEP:g}, nl_maxiter {NL_MAXITER})",
+            "nelmt": ne, "neq": neq,
+            "fos_model": "FOS solves/s = 1 / (plastic iterations per FOS solve x s per plastic iteration); "
+                         "iterations counted by a complete search of the 576-element cut of the same slope",
+            "l2": "inputs larger than L2 (FP32 element matrices 1.87 GB)", "parallelism": f"replicas{world}"}
+
+
+def golden_fos():
+    """The oracle's bisection on the cut (critical SRF, probes), or None."""
+    try:
+        with open(GOLDEN_FOS) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def oracle_fos_iterations():
+    """Trial plastic iterations of the oracle's bisection on the cut (the CPU
+    reference's own search); the bisection upper bound when no record exists."""
+    g = golden_fos()
+    if g:
+        return sum(p["nl_iter"] for p in g["probes"]), "oracle bisection on the 576-element cut"
+    return BISECT_TRIALS * NL_MAXITER, "upper bound: 8 bisection trials x nl_maxiter"
 
 
 def peaks():
@@ -135,9 +174,9 @@ def barrier(world: int):
 def oracle_sample(n_cg: float = N_CG_REF, iters: int = 30):
     """Time the oracle on a bounded sample of the workload and scale it to one
     plastic iteration of one trial on the full 192k-element mesh:
-    sample = the same slope geometry at 120x5x10 = 6,000 elements; 30 PCG
+    sample = the same slope geometry at 120x5x10 = 6,000 elements; `iters` PCG
     iterations (the reference EBE apply + vector ops) and one stress /
-    yield / body-load pass, scaled linearly by element and dof counts."""
+    yield / body-load pass, scaled linearly by element count."""
     import numpy as np
     from oracle.pyoracle import OracleModel, lib as olib
     from specfem3d_geotech_gb300 import meshgen
@@ -154,7 +193,6 @@ def oracle_sample(n_cg: float = N_CG_REF, iters: int = 30):
     t0 = time.perf_counter()
     olib().orc_pcg_solver(om.neq, om.nelmt, kflat, u, ext, dinv, ge, iters, 1e-300, ctypes.byref(it))
     t_pcg = (time.perf_counter() - t0) / iters
-    nm = om.nmatblk
     ym, nu = mesh.props[:, 1].copy(), mesh.props[:, 2].copy()
     phi, coh, psi = mesh.props[:, 3].copy(), mesh.props[:, 4].copy(), mesh.props[:, 5].copy()
     ev = np.zeros(om.nelmt * 27 * 6)
@@ -188,38 +226,39 @@ def cpu_reference(procs: int, n_cg: float = N_CG_REF):
     return rate, res
 
 
-# ---------------------------------------------------------------------------
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
     procs = max(1, min(os.cpu_count() or 1, 16))
     t0 = time.time()
     steps = []
-    rate = None
     res = None
     for i in range(args.warmup + args.steps):
         r, res = cpu_reference(procs)
         if i >= args.warmup:
             steps.append(r)
-        rate = r
     rate = statistics.median(steps)
-    value = rate / FOS_WORK
+    s_ref, s_src = oracle_fos_iterations()
+    value = rate / s_ref
     sample = (f"oracle (serial FP64 restatement of the reference path) on a 6,000-element cut of the same slope "
               f"(120x5x10): 30 PCG iterations + 1 stress pass per process, scaled by element count to 192k "
-              f"elements and to {N_CG_REF} PCG iterations per plastic iteration; {procs} independent processes")
+              f"elements and to {N_CG_REF} PCG iterations per plastic iteration; {procs} independent processes "
+              f"(independent trials); {s_ref} trial plastic iterations per FOS solve ({s_src})")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * (time.time() - t0) / max(1, args.steps + args.warmup),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "slope3d_192k FOS solve (120x40x40, NGLL=3, 4.63M dof)",
-                       "fos_work_model": f"{FOS_TRIALS} trials x {NL_MAXITER} plastic iterations"},
+            "config": workload_config(world),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "trial_plastic_iters_per_s": rate, "per_process": res}
+            "trial_plastic_iters_per_s": rate, "fos_plastic_iterations": s_ref, "per_process": res}
     print(json.dumps(line))
     return 0
 
 
+# ---------------------------------------------------------------------------
+# GPU legs
+# ---------------------------------------------------------------------------
 def apply_kernel_name(kr: int, nelmt: int) -> str:
     v = os.environ.get("SG_APPLY_VARIANT", "5")
     if v == "2" and kr in (8, 16):
@@ -231,19 +270,108 @@ def apply_kernel_name(kr: int, nelmt: int) -> str:
     return f"k_apply_sparse_tma<float,{kr}>"
 
 
-PREC_STEPS = 2               # plastic iterations compared by the precision leg
+PREC_STEPS = 2               # plastic iterations compared by the 192k precision check
 
 
-def precision_report(r64, x64, r32, x32):
-    """Mixed batched vs plain FP64 after the same plastic iterations at the same SRF."""
+def precision_192k(r64, x64, r32, x32):
+    """Mixed batched vs plain FP64 GPU on the 192k mesh after the same plastic
+    iterations at the same SRF (the full trials take hours there)."""
     import numpy as np
     d = np.linalg.norm(x32 - x64) / np.linalg.norm(x64)
     return {"plastic_iterations": PREC_STEPS, "srf": r64["srf"], "rel_l2_displacement": float(d),
             "rel_umax": abs(r32["umax"] - r64["umax"]) / abs(r64["umax"]),
-            "rel_fmax": abs(r32["fmax"] - r64["fmax"]) / max(abs(r64["fmax"]), 1e-300),
             "pcg_iters_fp64": r64["cg_tot"], "inner_pcg_iters_mixed": r32["cg_tot"],
             "pcg_inflation": r32["cg_tot"] / max(1, r64["cg_tot"]), "refine_rounds_mixed": r32["refine_steps"],
             "tolerance": 1e-6, "within_tolerance": bool(d <= 1e-6)}
+
+
+PREC_SRFS = (1.0, 1.2)       # whole trials of the cut compared field by field with the oracle
+
+
+def start_oracle_trials():
+    """Oracle trials of the cut at PREC_SRFS, started in spawned processes
+    before the first GPU call; they run on the host cores meanwhile."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import oracle_jobs
+    ex = cf.ProcessPoolExecutor(max_workers=len(PREC_SRFS), mp_context=mp.get_context("spawn"))
+    return ex, {s: ex.submit(oracle_jobs._trial, s) for s in PREC_SRFS}
+
+
+def precision_vs_oracle(sg, ctx, futures):
+    """Config-2 report against the FP64 oracle on the 576-element cut: the
+    mixed batched form (k trials in one batch) for whole trials at SRF 1.0
+    and 1.2 -- displacement L2, largest stress error, plastic-iteration
+    counts -- and at the oracle's critical SRF and the grid point below it
+    (the failing and the just-converging trial of its bisection), whose
+    summaries the oracle run in tests/golden holds."""
+    import numpy as np
+    from specfem3d_geotech_gb300 import meshgen
+    mesh = meshgen.slope3d(**CUT)
+    g = golden_fos()
+    srfs = list(PREC_SRFS)
+    near = []
+    if g:
+        crit = g["critical_srf"]
+        by = {round(p["srf"], 10): p for p in g["probes"]}
+        for s in (round(crit - SRF_STEP, 10), round(crit, 10)):
+            if s in by:
+                near.append(by[s])
+                srfs.append(s)
+    m = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=NL_MAXITER,
+                          precision=sg.PREC_MIXED)
+    res, x = m.trials(srfs, ctl, want_x=True)
+    stress = [m.last_stress(t) for t in range(len(PREC_SRFS))]
+    m.close()
+    out = {"mesh": f"slope3d cut {mesh.nelmt} elements", "form": f"mixed, {len(srfs)} trials in one batch",
+           "tolerance_displacement": 1e-6, "trials": []}
+    for t, s in enumerate(PREC_SRFS):
+        ro = futures[s].result()
+        smax = float(np.abs(ro["stress"]).max())
+        out["trials"].append({
+            "srf": s, "nl_iter_gpu": res[t]["nl_iter"], "nl_iter_oracle": ro["nl_iter"],
+            "rel_l2_displacement": float(np.linalg.norm(x[t] - ro["x"]) / np.linalg.norm(ro["x"])),
+            "max_stress_error_rel": float(np.abs(stress[t] - ro["stress"]).max() / smax),
+            "rel_umax": abs(res[t]["umax"] - ro["umax"]) / ro["umax"]})
+    for j, p in enumerate(near):
+        r = res[len(PREC_SRFS) + j]
+        out["trials"].append({
+            "srf": p["srf"], "nl_iter_gpu": r["nl_iter"], "nl_iter_oracle": p["nl_iter"],
+            "failed_gpu": r["failed"], "failed_oracle": p["failed"],
+            "rel_umax": abs(r["umax"] - p["umax"]) / p["umax"], "source": "oracle bisection record"})
+    out["within_tolerance"] = all(t.get("rel_l2_displacement", 0.0) <= 1e-6 for t in out["trials"])
+    out["same_iteration_counts"] = all(t["nl_iter_gpu"] == t["nl_iter_oracle"] for t in out["trials"])
+    return out
+
+
+def fos_measured(sg, ctx):
+    """Complete factor-of-safety searches on the 576-element cut of the same
+    slope (nl_maxiter 2000, SRF on [1, 3] to 0.01): the mixed batched form
+    (k = 8, refilled batch) and the plain FP64 form (bisection, one trial at
+    a time), each timed end to end, with the plastic iterations each ran."""
+    from specfem3d_geotech_gb300 import meshgen
+    mesh = meshgen.slope3d(**CUT)
+    out = {"mesh": f"slope3d cut {CUT['nx']}x{CUT['ny']}x{CUT['nz']} = {mesh.nelmt} elements",
+           "nl_maxiter": NL_MAXITER, "srf_grid": f"[{SRF_LO:g}, {SRF_HI:g}] step {SRF_STEP:g}"}
+    for name, prec, k in (("mixed_batched", sg.PREC_MIXED, K_TRIALS), ("plain_fp64", sg.PREC_FP64, 1)):
+        m = sg.Model(mesh, precision=prec, ctx=ctx)
+        ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=NL_MAXITER, precision=prec)
+        t0 = time.perf_counter()
+        fos, nt, nr = m.fos(ctl, SRF_LO, SRF_HI, SRF_STEP, k=k)
+        t = time.perf_counter() - t0
+        out[name] = {"fos": round(fos, 10), "k": k, "trials": nt, "plastic_iterations": m.fos_steps(),
+                     "seconds": t, "fos_solves_per_s": 1.0 / t}
+        m.close()
+    g = golden_fos()
+    if g:
+        out["oracle"] = {"fos": g["critical_srf"], "trials": len(g["probes"]),
+                         "plastic_iterations": sum(p["nl_iter"] for p in g["probes"]),
+                         "seconds": g["oracle_seconds"], "source": "tests/golden/slope3d_cut_fos.json"}
+    crit = {out["mixed_batched"]["fos"], out["plain_fp64"]["fos"]} | ({g["critical_srf"]} if g else set())
+    out["same_critical_srf"] = len(crit) == 1
+    out["fos_level_speedup"] = out["plain_fp64"]["seconds"] / out["mixed_batched"]["seconds"]
+    return out
 
 
 def serving_leg(sg, args):
@@ -320,35 +448,36 @@ def plain_fp64(sg, ctx, mesh, srf0, args, want_x=False):
     return steps64 / (t64 / 1000.0), (a64["cg_tot"] - b64["cg_tot"]) / max(1, steps64), px
 
 
-def end_to_end(sg, ctx, mesh, ctl, srf, k, args, world):
-    """The same work through the public API from host buffers: mesh H2D +
-    device model build, the k trials for e2e_steps plastic iterations, result D2H."""
-    e2e_steps = max(1, args.steps // 2)
+def end_to_end(sg, ctx, mesh, srf, k, args, s_mixed, world):
+    """The same work through the public API from host buffers: mesh H2D,
+    device model build, the k trials for e2e_steps plastic iterations and the
+    k displacement vectors copied back (the drop-in's result, x)."""
+    e2e_steps = max(2, args.steps // 2)
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=e2e_steps, precision=sg.PREC_MIXED)
     t0 = time.perf_counter()
     me = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
-    me.batch_begin(ctl, k)
-    for s in srf:
-        me.batch_add(s)
-    me.batch_step(e2e_steps)
-    res = [me.batch_poll(t)[1] for t in range(k)]
-    me.batch_end()
+    _, x = me.trials(srf, ctl, want_x=True)
     t_e2e = time.perf_counter() - t0
     me.close()
-    slot_steps = sum(r["nl_iter"] for r in res)
     h2d = sum(a.nbytes for a in (mesh.x, mesh.y, mesh.z, mesh.conn, mesh.mat_id, mesh.props)) + \
         sum(b.nbytes for b in mesh.bc)
-    return (slot_steps / t_e2e) * world / FOS_WORK, h2d, t_e2e, e2e_steps
+    value = world / (s_mixed * t_e2e / e2e_steps)
+    return {"value": value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
+            "d2h_bytes_per_step": x.nbytes / e2e_steps, "seconds": t_e2e, "steps": e2e_steps,
+            "includes": "mesh upload, device model build (stiffness), cold-start plastic iterations, x download"}
 
 
 def run_ours(args, rank, world, local):
     import numpy as np
+    # oracle trials for the precision report start before any GPU call
+    oex, ofut = (None, None) if (args.no_fp64 or rank != 0) else start_oracle_trials()
     import specfem3d_geotech_gb300 as sg
     from specfem3d_geotech_gb300 import build, meshgen
     build.build()
     ctx = sg.Context(local)
     mesh = meshgen.slope3d(nx=args.nx, seed=1 + rank)
     k = args.k
-    srf = [1.0 + 2.0 * (t + 1) / (k + 1) for t in range(k)]   # first k-section round on [1, 3]
+    srf = [1.0 + 2.0 * (t + 1) / (k + 1) for t in range(k)]   # the first probes of a search on [1, 3]
 
     # ---- mixed-precision batched form, inputs resident -------------------
     model = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
@@ -380,16 +509,27 @@ def run_ours(args, rank, world, local):
     model.batch_end()
     prec32 = None
     if not args.no_fp64:
-        # config-2 precision report: the same batch of k trials, first PREC_STEPS plastic iterations
         cp = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=PREC_STEPS,
                              precision=sg.PREC_MIXED)
         r, x = model.trials(srf, cp, want_x=True)
         prec32 = (r[0], x[0])
     t_max = barrier_max(t_ms, world)
-    rate_all = slot_steps / (t_max / 1000.0) * world         # trial plastic iterations / s, all ranks
-    value = rate_all / FOS_WORK
+    step_s = t_max / args.steps / 1000.0                      # seconds per batch plastic iteration
+    rate_all = slot_steps / (t_max / 1000.0) * world          # trial plastic iterations / s, all ranks
     ne, neq = model.nelmt, model.neq
     model.close()
+
+    # ---- plastic iterations per FOS solve: complete searches on the cut ----
+    fosm = None if args.no_fos else fos_measured(sg, ctx)
+    if fosm:
+        s_mixed = fosm["mixed_batched"]["plastic_iterations"]
+        s_plain = fosm["plain_fp64"]["plastic_iterations"]
+        count_src = "measured: complete searches on the 576-element cut in this run"
+    else:
+        s_mixed = 3 * NL_MAXITER                  # k-section bound: 3 rounds of 8 on 200 steps
+        s_plain = BISECT_TRIALS * NL_MAXITER
+        count_src = "upper bounds: 3 rounds x nl_maxiter (batched), 8 trials x nl_maxiter (bisection)"
+    value = world / (s_mixed * step_s)
 
     # roofline of the dominant kernel: the batched FP32 element apply (k RHS)
     hbm, peak_kind = peaks()
@@ -411,30 +551,28 @@ def run_ours(args, rank, world, local):
     else:
         rate64, n_cg_ref, prec64 = plain_fp64(sg, ctx, mesh, srf[0], args, want_x=True)
         rate64 *= world
-        precision = precision_report(prec64[0], prec64[1], prec32[0], prec32[1])
-    if args.no_e2e:
-        e2e = None
-    else:
-        e2e_value, h2d, t_e2e, e2e_steps = end_to_end(sg, ctx, mesh, ctl, srf, k, args, world)
-        e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d / e2e_steps,
-               "d2h_bytes_per_step": k * 80 / e2e_steps, "seconds": t_e2e, "steps": e2e_steps}
+        precision = {"vs_fp64_oracle_576": precision_vs_oracle(sg, ctx, ofut) if ofut else None,
+                     "vs_fp64_gpu_192k": precision_192k(prec64[0], prec64[1], prec32[0], prec32[1])}
+    value64 = rate64 / s_plain
+    e2e = None if args.no_e2e else end_to_end(sg, ctx, mesh, srf, k, args, s_mixed, world)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": f"slope3d_{ne // 1000}k ({args.nx}x40x40 hex, NGLL=3, {neq} dof), mixed "
-                               f"FP32/FP64-refined, {k} concurrent SRF trials", "nelmt": ne, "neq": neq,
-                   "k_trials": k, "step": f"one plastic iteration of the {k}-trial batch",
-                   "fos_work_model": f"{FOS_TRIALS} trials x {NL_MAXITER} plastic iterations per FOS solve",
-                   "l2": "inputs larger than L2 (FP32 element matrices 1.87 GB)", "parallelism": f"replicas{world}"},
+        "config": workload_config(world, ne, neq, args.nx),
+        "form": {"k_trials": k, "step": f"one plastic iteration of the {k}-trial batch",
+                 "search": "sg_fos, k = 8: refilled batch (converged trials raise, failed trials lower the bracket)"},
+        "fos_plastic_iterations": {"mixed_batched": s_mixed, "plain_fp64": s_plain, "source": count_src},
         "trial_plastic_iters_per_s": rate_all,
         "pcg_iters_per_step": cg / max(1, args.steps),
         "latency": {"step_p50_ms": float(np.percentile(step_ms, 50)),
                     "step_p99_ms": float(np.percentile(step_ms, 99))},
-        "fp64_plain": {"trial_plastic_iters_per_s": rate64, "value": rate64 / FOS_WORK,
+        "fp64_plain": {"trial_plastic_iters_per_s": rate64, "value": value64,
                        "pcg_iters_per_plastic_iter": n_cg_ref,
-                       "mixed_batched_over_plain": rate_all / rate64 if rate64 == rate64 else None},
+                       "mixed_batched_over_plain_per_trial_iteration": rate_all / rate64 if rate64 == rate64 else None,
+                       "mixed_batched_over_plain_fos": value / value64 if value64 == value64 else None},
+        "fos_measured": fosm,
         "precision": precision,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": apply_kernel_name(kr, ne),
@@ -452,14 +590,17 @@ def run_ours(args, rank, world, local):
         line["serving"] = serving_leg(sg, args)
     if rank == 0 and not args.no_cpu:
         t0 = time.time()
-        r = oracle_sample(n_cg=n_cg_ref, iters=CPU_SAMPLE_ITERS)
+        r = oracle_sample(n_cg=N_CG_REF, iters=CPU_SAMPLE_ITERS)
+        s_ref, s_src = oracle_fos_iterations()
         cpu_rate = 1.0 / r["t_plastic_iter_full"]
         line["cpu_baseline"] = {
-            "value": cpu_rate / FOS_WORK, "unit": UNIT, "cores": 1, "kind": "port",
+            "value": cpu_rate / s_ref, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": (f"oracle on a 6,000-element cut of the same slope ({CPU_SAMPLE_ITERS} PCG iterations + "
-                       f"1 stress pass, "
-                       f"{time.time() - t0:.0f} s), scaled by element count to 192k elements and to "
-                       f"{n_cg_ref:.0f} PCG iterations per plastic iteration")}
+                       f"1 stress pass, {time.time() - t0:.0f} s), scaled by element count to 192k elements and to "
+                       f"{N_CG_REF} PCG iterations per plastic iteration; {s_ref} trial plastic iterations per "
+                       f"FOS solve ({s_src})")}
+    if oex is not None:
+        oex.shutdown(wait=False, cancel_futures=True)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -474,8 +615,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--k", type=int, default=K_TRIALS)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU oracle baseline")
-    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison and precision report")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--no-fos", action="store_true", help="skip the complete searches on the 576-element cut")
     ap.add_argument("--nx", type=int, default=120, help="elements along x (120 = the 192k-element mesh)")
     ap.add_argument("--serve", type=int, default=6, help="requests in the serving leg (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving leg (1/s)")
