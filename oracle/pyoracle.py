@@ -234,6 +234,8 @@ class OracleModel:
         sf = np.zeros(self.nnode) if want_fields else None
         n = lib().orc_excavation(self.h, s0_type, z0, s0, k0, nexcav, nexcavid, excavid, ninc, srf, res, None,
                                  None if vm is None else vm.ctypes.data, None if sf is None else sf.ctypes.data)
+        if n == -2:
+            raise ValueError("excavation stage list passes the end of excavid")
         if want_fields:
             return res.reshape(-1, 8)[:n], vm, sf
         return res.reshape(-1, 8)[:n]

@@ -1663,6 +1663,13 @@ int orc_excavation(void* hv, int s0_type, double z0, double s0, double k0, int n
                    const int* excavid, int ninc, double srf, double* res, double* x_last, double* vmeps_out,
                    double* scf_out) {
   OrcModel* h = (OrcModel*)hv;
+  {
+    // the stage index of src/excavation.F90:339 must stay inside excavid
+    long long total = 0;
+    for (int is = 0; is < nexcav; ++is) total += nexcavid[is];
+    for (int is = 0; is < nexcav; ++is)
+      if (nexcavid[is] < 1 || (long long)is * nexcavid[is] + nexcavid[is] > total) return -2;
+  }
   Model M = h->M;  // gdof is renumbered per stage
   const Control& C = h->C;
   const int nel = M.nelmt, nm = M.nmatblk;

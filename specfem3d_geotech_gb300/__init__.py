@@ -608,6 +608,8 @@ class Model:
                    nexcavid: Optional[Sequence[int]] = None, ninc: int = 1, srf: float = 1.0):
         excavid = np.ascontiguousarray(excavid, np.int32)
         nexcavid = np.ones(len(excavid), np.int32) if nexcavid is None else np.ascontiguousarray(nexcavid, np.int32)
+        if int(nexcavid.sum()) != excavid.size:
+            raise ValueError("excavid must list sum(nexcavid) material ids")
         res = np.zeros(8 * len(nexcavid))
         n = C.c_int(0)
         st = lib().sg_excavation(self.h, C.byref(ctl), s0_type, z0, s0, k0, len(nexcavid), _ptr(nexcavid),

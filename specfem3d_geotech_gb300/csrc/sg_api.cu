@@ -1597,6 +1597,23 @@ extern "C" int sg_excavation(sg_model* M, const sg_control* ctl, int s0_type, do
                              int nexcav, const int* nexcavid, const int* excavid, int ninc, double srf,
                              double* stage_res, int* nstage) {
   if (!M || !ctl || nexcav < 1 || !nexcavid || !excavid || ninc < 1 || !stage_res) return SG_ERR_BADARG;
+  {
+    // Stage i removes excavid(id0 .. id0 + nexcavid(i) - 1) with id0 =
+    // (i-1)*nexcavid(i) + 1 (src/excavation.F90:339).  With unequal counts
+    // that index can pass the end of excavid (sum of nexcavid entries), where
+    // the reference reads past its array; such a list is refused here.
+    long long total = 0;
+    for (int is = 0; is < nexcav; ++is) {
+      if (nexcavid[is] < 1) { M->ctx->err = "nexcavid entries must be positive"; return SG_ERR_BADARG; }
+      total += nexcavid[is];
+    }
+    for (int is = 0; is < nexcav; ++is)
+      if ((long long)is * nexcavid[is] + nexcavid[is] > total) {
+        M->ctx->err = "stage " + std::to_string(is + 1) +
+                      ": (stage-1)*nexcavid(stage)+nexcavid(stage) passes the end of excavid";
+        return SG_ERR_BADARG;
+      }
+  }
   sg_ctx* c = M->ctx;
   HostMesh& h = M->H;
   cudaSetDevice(c->device);

@@ -145,10 +145,6 @@ struct Shape {
 __device__ __forceinline__ void cp_async4(int* dst, const int* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
-__device__ __forceinline__ void prefetch_l2(const float* a) {
-  asm volatile("prefetch.L2 [%0];" ::"l"(a));
-}
-constexpr int PF_CHUNK = 3;    // chunk after which the next group's p and z rows are prefetched
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
@@ -262,26 +258,6 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
       const float4* src = reinterpret_cast<const float4*>(mine + (C % NSTAGE) * S::STAGE_F);
       chunk_entries<C>(src, p, y, std::make_integer_sequence<int, (C == NCH - 1) ? LAST_F4 : CHF / 4>{});
       __syncwarp();
-      // A third of the way through the group the next group's dof numbers
-      // (copied since this group started) are waited for, and the rows of
-      // p_old and z its lanes will gather are prefetched into L2: at the
-      // next group's start those loads then come from L2 instead of HBM.
-      // A prefetch moves no data into registers.
-      if constexpr (C == PF_CHUNK) {
-        cp_async_wait_all();
-        __syncwarp();
-        const int gn = g + gstride;
-        if (gn < ngroups) {
-          const int* nb = ibuf + (buf ^ 1) * (S::EPW * IDX);
-          const int nv = min(S::EPW, nelmt - gn * S::EPW);
-          for (int t = lane; t < nv * NEDOF; t += 32) {
-            const int ii = t / NEDOF, r = t - ii * NEDOF;
-            const int gd = nb[ii * IDX + r];
-            prefetch_l2(pold + (size_t)gd * KR);
-            if (combine) prefetch_l2(z + (size_t)gd * KR);
-          }
-        }
-      }
     };
     for_chunks(step, std::make_integer_sequence<int, NCH>{});
     if (!ok) break;
