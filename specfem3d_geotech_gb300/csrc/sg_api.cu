@@ -260,7 +260,28 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
   int it = 0;
   int status = SG_OK;
   volatile PcgGlobal* hG = (volatile PcgGlobal*)C->pin;
+  // FP32, 8 or 16 columns, stored matrices applied by k_apply_lanes, residual
+  // test: two kernels per iteration (the apply forms the direction from the
+  // previous step's r and kp; k_pcg_gather_update does the rest)
+  bool fused = false;
+  if constexpr (std::is_same<V, float>::value && (KR == 8 || KR == 16))
+    fused = (mode & 1) && apply_uses_lanes(op.dense, KR) && fused_pcg_enabled();
   auto eager_chunk = [&]() {
+    if constexpr (std::is_same<V, float>::value && (KR == 8 || KR == 16)) {
+      if (fused) {
+        for (int c = 0; c < chunk; ++c) {
+          ev = C->prof_begin();
+          launch_apply_lanes<KR>((const float*)op.K, op.ge, op.nelmt, B.p, nullptr, 2, B.Y, B.cs, B.G, op.T->d_pos,
+                                 &B.G->err, s, FusedDir{B.r, B.kp, dp});
+          add_launches(1);
+          C->prof_end(ev, 1);
+          ev = C->prof_begin();
+          pcg_gather_update<KR>(*op.T, B.Y, B.kp, B.p, B.r, u, dp, B.cs, B.G, B.part, s);
+          C->prof_end(ev, 2);
+        }
+        return;
+      }
+    }
     for (int c = 0; c < chunk; ++c) {
       ev = C->prof_begin();
       pcg_apply<V, KR>(op.dense, op.K, op.ge, op.nelmt, B.p, B.z, 1, B.Y, B.cs, B.G, C->d_nbr, op.T->d_pos,
@@ -283,7 +304,7 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
       (uintptr_t)op.T->d_ent, (uintptr_t)op.T->d_dof, (uintptr_t)op.T->d_pos, (uintptr_t)op.T->ngroups,
       (uintptr_t)C->d_nbr, (uintptr_t)B.Y, (uintptr_t)B.kp, (uintptr_t)B.p, (uintptr_t)B.z, (uintptr_t)B.r,
       (uintptr_t)B.cs, (uintptr_t)B.G, (uintptr_t)B.part, (uintptr_t)u, (uintptr_t)f, (uintptr_t)dp,
-      (uintptr_t)n1, (uintptr_t)KR, (uintptr_t)sizeof(V), (uintptr_t)chunk, (uintptr_t)0};
+      (uintptr_t)n1, (uintptr_t)KR, (uintptr_t)sizeof(V), (uintptr_t)chunk, (uintptr_t)fused};
   // very small meshes with the matrix-free FP32 operator: the whole chunk as
   // one persistent cooperative launch (sg_pcg_persist.cu), below the size at
   // which the grid barrier costs more than the launches it saves
@@ -301,7 +322,7 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
     if (done_chunk) {
     } else if (ex) {
       cudaGraphLaunch(ex, s);
-      add_launches(3LL * chunk);
+      add_launches((fused ? 2LL : 3LL) * chunk);
     } else {
       eager_chunk();
     }

@@ -188,7 +188,7 @@ template <int KR>
 __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
     const float* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const float* __restrict__ pold,
     const float* __restrict__ z, int combine, float* __restrict__ Y, const ColState* __restrict__ cs,
-    const PcgGlobal* __restrict__ G, const int* __restrict__ pos, int* __restrict__ err) {
+    const PcgGlobal* __restrict__ G, const int* __restrict__ pos, int* __restrict__ err, FusedDir fz) {
   using S = Shape<KR>;
   if (G && G->all_done) return;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -206,6 +206,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
   }
   __syncthreads();
   const float beta = combine ? (float)cs[j].beta : 0.f;
+  const float alpha = combine == 2 ? (float)cs[j].alpha : 0.f;
   // chunks issued / waited, counted along the warp's chunk sequence
   int issued = 0, waited = 0;
   if (lane == 0)
@@ -230,7 +231,13 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
       for (int r = 0; r < NEDOF; ++r) {
         const int gd = valid ? idx[r] : 0;
         float pv = pj[(size_t)gd * KR];
-        if (combine) pv = fmaf(beta, pv, zj[(size_t)gd * KR]);
+        if (combine == 1) {
+          pv = fmaf(beta, pv, zj[(size_t)gd * KR]);
+        } else if (combine == 2) {
+          // z of this iteration from the previous step: D (r - alpha kp)
+          const float zv = fz.dinv[gd] * fmaf(-alpha, fz.kp[(size_t)gd * KR + j], fz.r[(size_t)gd * KR + j]);
+          pv = fmaf(beta, pv, zv);
+        }
         p[r] = valid ? pv : 0.f;
         y[r] = 0.f;
       }
@@ -285,7 +292,8 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
 
 template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
-                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s) {
+                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
+                        FusedDir fz) {
   using S = lanes::Shape<KR>;
   static bool attr = false;
   if (!attr) {
@@ -296,7 +304,7 @@ void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* 
   const int warps = (ngroups + lanes::NW - 1) / lanes::NW;
   int grid = warps < 152 ? warps : 152;
   if (grid < 1) return;
-  lanes::k_apply_lanes<KR><<<grid, lanes::NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, combine, Y, cs, G, pos, err);
+  lanes::k_apply_lanes<KR><<<grid, lanes::NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, combine, Y, cs, G, pos, err, fz);
 }
 
 size_t apply_lanes_smem(int KR) {
@@ -304,8 +312,8 @@ size_t apply_lanes_smem(int KR) {
 }
 
 template void launch_apply_lanes<8>(const float*, const int*, int, const float*, const float*, int, float*,
-                                    const ColState*, const PcgGlobal*, const int*, int*, cudaStream_t);
+                                    const ColState*, const PcgGlobal*, const int*, int*, cudaStream_t, FusedDir);
 template void launch_apply_lanes<16>(const float*, const int*, int, const float*, const float*, int, float*,
-                                     const ColState*, const PcgGlobal*, const int*, int*, cudaStream_t);
+                                     const ColState*, const PcgGlobal*, const int*, int*, cudaStream_t, FusedDir);
 
 }  // namespace sg

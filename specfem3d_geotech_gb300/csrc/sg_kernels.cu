@@ -16,6 +16,7 @@
 // All reductions use a fixed grid (NPART blocks) and fixed-order trees, so a
 // run is bitwise reproducible on the same device type.
 #include <cstdio>
+#include <cstdlib>
 #include <algorithm>
 #include <type_traits>
 
@@ -1025,6 +1026,208 @@ __global__ void __launch_bounds__(RED_THREADS, 4) k_pcg_gather_rows(
   }
 }
 
+// Fused FP32 PCG step for 8 or 16 columns (residual-reduction mode): with
+// the element apply forming p_k = beta_k p_{k-1} + D (r_{k-1} - alpha_{k-1}
+// kp_{k-1}) on the fly, one kernel per step does the rest of src/solver.f90:
+// 53-73 for every free dof row (node, dof, four columns):
+//   q = kp_k   = sum of the row's element products in element order
+//   u += alpha_{k-1} p_{k-1},  r_k = r_{k-1} - alpha_{k-1} kp_{k-1},  z_k = D r_k,
+//   p_k = beta_k p_{k-1} + z_k   (bitwise the p_k of the apply)
+// and the partial sums p_k.q, q.z_k, q.(D q), r_k.r_k and max|p_k|.  The last
+// block stops a column when r_k.r_k <= tol^2 r_0.r_0 (k-1 completed steps);
+// otherwise alpha_k = gamma_k / p_k.q and, without forming r_{k+1},
+//   gamma_{k+1} = r_{k+1}.z_{k+1} = gamma_k - 2 alpha_k q.z_k + alpha_k^2 q.(D q),
+//   beta_{k+1} = gamma_{k+1} / gamma_k.
+// So an iteration is two kernels (apply, this) instead of three, and u, r,
+// z and kp make one trip through HBM fewer.  The dots use the compensated
+// FP32 sums of the other kernels; r.r only feeds the stop test and is summed
+// plainly.
+constexpr int GU_NQ = 8;                 // partial quantities per column (5 used)
+constexpr int GU_BLOCKS = 152 * 2;       // two resident CTAs per SM (128 registers)
+
+template <int KR>
+__global__ void __launch_bounds__(RED_THREADS, 2) k_pcg_gather_update(
+    const int* __restrict__ ptr, const int* __restrict__ dof, int ng, const float* __restrict__ Y,
+    float* __restrict__ kp, float* __restrict__ p, float* __restrict__ r, float* __restrict__ u,
+    const float* __restrict__ dinv, ColState* __restrict__ cs, PcgGlobal* __restrict__ G, double* __restrict__ part) {
+  if (G->all_done) return;
+  constexpr int QPD = KR / 4;      // 16-byte pieces per dof row
+  constexpr int LPN = 3 * QPD;     // lanes per node
+  constexpr int NPW = 32 / LPN;    // nodes per warp
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nl = lane / LPN, q = lane - nl * LPN;
+  const int d = q / QPD, c0 = 4 * (q - d * QPD);
+  const bool act = nl < NPW;
+  bool live[4];
+  float alpha[4], beta[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int j = act ? c0 + k : 0;
+    live[k] = act && cs[j].active && !cs[j].done;
+    alpha[k] = (float)cs[j].alpha;
+    beta[k] = (float)cs[j].beta;
+  }
+  DotAcc<float> sd[4], sa[4], sb[4];
+  float srr[4] = {0.f, 0.f, 0.f, 0.f}, smp[4] = {0.f, 0.f, 0.f, 0.f};
+  const float4* yq = reinterpret_cast<const float4*>(Y) + q;
+  const int wstride = gridDim.x * GATHER_WARPS * NPW;
+  for (int g0 = (blockIdx.x * GATHER_WARPS + warp) * NPW; g0 < ng; g0 += wstride) {
+    const int g = g0 + nl;
+    if (!act || g >= ng) continue;
+    const int a = ptr[g], b = ptr[g + 1];
+    const int gd = dof[3 * g + d];
+    const size_t o = (size_t)gd * KR + c0;
+    float4 pv = make_float4(0.f, 0.f, 0.f, 0.f), rv = pv, kv = pv, uv = pv;
+    float dv = 0.f;
+    if (gd) {
+      pv = *reinterpret_cast<const float4*>(p + o);
+      rv = *reinterpret_cast<const float4*>(r + o);
+      kv = *reinterpret_cast<const float4*>(kp + o);
+      uv = *reinterpret_cast<const float4*>(u + o);
+      dv = dinv[gd];
+    }
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (a + k < b) v[k] = __ldcs(yq + (size_t)(a + k) * LPN);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (a + k < b) {
+        acc.x = acc.x + v[k].x;
+        acc.y = acc.y + v[k].y;
+        acc.z = acc.z + v[k].z;
+        acc.w = acc.w + v[k].w;
+      }
+    for (int sl = a + 4; sl < b; ++sl) {
+      const float4 w = __ldcs(yq + (size_t)sl * LPN);
+      acc.x = acc.x + w.x;
+      acc.y = acc.y + w.y;
+      acc.z = acc.z + w.z;
+      acc.w = acc.w + w.w;
+    }
+    if (!gd) continue;
+    float pa[4] = {pv.x, pv.y, pv.z, pv.w}, ra[4] = {rv.x, rv.y, rv.z, rv.w};
+    float ka[4] = {kv.x, kv.y, kv.z, kv.w}, ua[4] = {uv.x, uv.y, uv.z, uv.w};
+    const float qa[4] = {acc.x, acc.y, acc.z, acc.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (!live[k]) continue;          // stopped or inactive columns keep u, r and p
+      const float un = fmaf(alpha[k], pa[k], ua[k]);
+      const float rn = fmaf(-alpha[k], ka[k], ra[k]);
+      const float zn = dv * rn;
+      const float pn = fmaf(beta[k], pa[k], zn);
+      sd[k].add(pn, qa[k]);
+      sa[k].add(qa[k], zn);
+      sb[k].add(qa[k], dv * qa[k]);
+      srr[k] = fmaf(rn, rn, srr[k]);
+      smp[k] = fmaxf(smp[k], fabsf(pn));
+      ua[k] = un; ra[k] = rn; pa[k] = pn;
+    }
+    *reinterpret_cast<float4*>(u + o) = make_float4(ua[0], ua[1], ua[2], ua[3]);
+    *reinterpret_cast<float4*>(r + o) = make_float4(ra[0], ra[1], ra[2], ra[3]);
+    *reinterpret_cast<float4*>(p + o) = make_float4(pa[0], pa[1], pa[2], pa[3]);
+    *reinterpret_cast<float4*>(kp + o) = acc;
+  }
+  // block partials: [block][column][GU_NQ] = p.q, q.z, q.Dq, r.r, max|p|
+  __shared__ double sred[RED_THREADS / 32][KR][5];
+  auto mine = [&](int k, int qq) -> double {
+    if (!(act && live[k])) return 0.0;
+    return qq == 0 ? sd[k].value() : qq == 1 ? sa[k].value() : qq == 2 ? sb[k].value()
+                   : qq == 3 ? (double)srr[k] : (double)smp[k];
+  };
+#pragma unroll
+  for (int j = 0; j < KR; ++j) {
+    const bool own = act && (j >> 2) == (c0 >> 2);
+#pragma unroll
+    for (int qq = 0; qq < 5; ++qq) {
+      double v = own ? mine(j & 3, qq) : 0.0;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const double w = __shfl_xor_sync(FULL, v, o);
+        v = (qq == 4) ? fmax(v, w) : v + w;
+      }
+      if (lane == 0) sred[warp][j][qq] = v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < KR * 5) {
+    const int j = threadIdx.x / 5, qq = threadIdx.x % 5;
+    double v = 0.0;
+    for (int w = 0; w < RED_THREADS / 32; ++w) v = (qq == 4) ? fmax(v, sred[w][j][qq]) : v + sred[w][j][qq];
+    part[((size_t)blockIdx.x * KR + j) * GU_NQ + qq] = v;
+  }
+  if (!last_block(&G->cntB)) return;
+  // fixed-order reduction of the block partials: thread t owns quantity t % GU_NQ
+  __shared__ double sfin[RED_THREADS];
+  __shared__ int s_alldone;
+  {
+    constexpr int NQ = GU_NQ * KR;
+    static_assert(RED_THREADS % NQ == 0, "a thread keeps one quantity");
+    const int qq = threadIdx.x % GU_NQ;
+    double v = 0.0;
+    for (int idx = threadIdx.x; idx < (int)gridDim.x * NQ; idx += RED_THREADS) {
+      const double x = __ldcg(part + idx);
+      v = (qq == 4) ? fmax(v, x) : v + x;
+    }
+    sfin[threadIdx.x] = v;
+  }
+  if (threadIdx.x == 0) s_alldone = 1;
+  __syncthreads();
+  const int it = G->it + 1;
+  if (threadIdx.x < KR) {
+    constexpr int NQ = GU_NQ * KR;
+    const int jj = threadIdx.x;
+    ColState& c = cs[jj];
+    double pq = 0.0, qz = 0.0, qdq = 0.0, rr = 0.0, mp = 0.0;
+    for (int t = jj * GU_NQ; t < RED_THREADS; t += NQ) {
+      pq += sfin[t]; qz += sfin[t + 1]; qdq += sfin[t + 2]; rr += sfin[t + 3]; mp = fmax(mp, sfin[t + 4]);
+    }
+    if (c.active && !c.done) {
+      c.rr = rr;
+      if (rr <= c.tol * c.tol * c.rr0) {
+        c.done = 1; c.iters = it - 1;          // alpha and maxp stay those of the last step taken
+      } else if (it - 1 >= G->maxiter) {
+        c.done = 1; c.failed = 1; c.iters = G->maxiter + 1;
+      } else {
+        const double al = c.rz / pq;
+        const double gn = c.rz - 2.0 * al * qz + al * al * qdq;
+        c.alpha = al;
+        c.beta = gn / c.rz;
+        c.rz = gn;
+        c.maxp = mp;
+      }
+    }
+    if (jj < G->kcols && c.active && !c.done) atomicAnd(&s_alldone, 0);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    G->it = it;
+    G->all_done = s_alldone;
+    G->cntB = 0;
+  }
+}
+
+template <int KR>
+void pcg_gather_update(const GatherTopo& T, const float* Y, float* kp, float* p, float* r, float* u,
+                       const float* dinv, ColState* cs, PcgGlobal* G, double* part, cudaStream_t s) {
+  constexpr int NPB = GATHER_WARPS * (32 / (3 * KR / 4));       // nodes per block and pass
+  constexpr int CAP_PART = NPART * 16 * 4 / (GU_NQ * KR);       // blocks whose partials fit
+  constexpr int CAP = CAP_PART < GU_BLOCKS ? CAP_PART : GU_BLOCKS;
+  SG_LAUNCH k_pcg_gather_update<KR><<<red_grid(T.ngroups, NPB * 4, CAP), RED_THREADS, 0, s>>>(
+      T.d_ptr, T.d_dof, T.ngroups, Y, kp, p, r, u, dinv, cs, G, part);
+}
+template void pcg_gather_update<8>(const GatherTopo&, const float*, float*, float*, float*, float*, const float*,
+                                   ColState*, PcgGlobal*, double*, cudaStream_t);
+template void pcg_gather_update<16>(const GatherTopo&, const float*, float*, float*, float*, float*, const float*,
+                                    ColState*, PcgGlobal*, double*, cudaStream_t);
+
+bool fused_pcg_enabled() {
+  static const bool on = !(getenv("SG_FUSED") && atoi(getenv("SG_FUSED")) == 0);
+  return on;
+}
+bool apply_uses_lanes(int dense, int KR) { return dense == 0 && (KR == 8 || KR == 16) && g_apply_variant >= 3; }
+
 template <typename V, int KR>
 void pcg_gather(const GatherTopo& T, const V* Y, V* kp, V* p, const V* z, int mode, ColState* cs, PcgGlobal* G,
                 double* part, cudaStream_t s) {
@@ -1124,6 +1327,7 @@ __device__ __forceinline__ void update_finish(int init, ColState* __restrict__ c
         // keep_dir (G->mode & 2): continue the previous search direction after a
         // residual replacement, beta = r.z_new / r.z of the last completed step
         c.beta = (G->mode & 2) ? s / c.rz : 0.0;
+        c.alpha = 0.0;   // the fused step's first vector update is empty
         c.rz = s; c.rr0 = q; c.rr = q; c.done = 0; c.failed = 0; c.iters = 0;
       } else {
         c.done = 1;

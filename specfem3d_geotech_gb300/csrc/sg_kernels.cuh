@@ -54,9 +54,26 @@ template <int KR>
 void launch_apply_tc(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
                      float* Y, const ColState* cs, const PcgGlobal* G, const int* d_entry, const int* pos,
                      int* err, cudaStream_t s);
+// The search direction formed inside the fused FP32 iteration (combine = 2):
+// p = beta p_old + D (r - alpha kp) from the previous step's r, kp and the
+// inverted diagonal D, so that the vector update needs no kernel of its own.
+struct FusedDir {
+  const float* r = nullptr;
+  const float* kp = nullptr;
+  const float* dinv = nullptr;
+};
 template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
-                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s);
+                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
+                        FusedDir fz = FusedDir());
+// Fused FP32 PCG step for 8 or 16 columns (see k_pcg_gather_update): gather
+// of the element products, the previous step's vector update, the new
+// direction and the dots of the next step in one kernel.
+template <int KR>
+void pcg_gather_update(const GatherTopo& T, const float* Y, float* kp, float* p, float* r, float* u,
+                       const float* dinv, ColState* cs, PcgGlobal* G, double* part, cudaStream_t s);
+bool fused_pcg_enabled();   // SG_FUSED=0 keeps the three-kernel iteration
+bool apply_uses_lanes(int dense, int KR);  // the FP32 apply of this operator is k_apply_lanes
 // Matrix-free FP32 apply (sg_apply_mf.cu): rec holds per GLL point J^-1 and the
 // C constants times w detJ; pcg_apply takes it with dense = 2.
 template <int KR>

@@ -302,7 +302,7 @@ def test_tensor_core_apply_matches_simt(ctx, tmp_path):
         assert rel(d["x"][t], x1[t]) <= MIXED_TOL
 
 
-def _variant_trials(variant, srfs, out, var="SG_APPLY_VARIANT"):
+def _variant_trials(variant, srfs, out, var="SG_APPLY_VARIANT", extra=None):
     import subprocess
     import sys
     code = ("import sys; sys.path.insert(0, %r); import numpy as np; import specfem3d_geotech_gb300 as sg;"
@@ -311,6 +311,7 @@ def _variant_trials(variant, srfs, out, var="SG_APPLY_VARIANT"):
             "np.savez(%r, x=x, nl=np.array([t['nl_iter'] for t in r]), cg=np.array([t['cg_tot'] for t in r]))") % (
         os.path.dirname(os.path.dirname(os.path.abspath(__file__))), srfs, str(out))
     env = dict(os.environ)
+    env.update(extra or {})
     env[var] = str(variant)
     subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=600)
     return np.load(out)
@@ -326,6 +327,23 @@ def test_lane_apply_matches_node_lane_apply(tmp_path, k):
     a = _variant_trials(1, srfs, tmp_path / "v1.npz")
     b = _variant_trials(3, srfs, tmp_path / "v3.npz")
     c = _variant_trials(3, srfs, tmp_path / "v3b.npz")
+    assert a["nl"].tolist() == b["nl"].tolist()
+    for t in range(k):
+        assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
+    assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
+
+
+@pytest.mark.parametrize("k", [8, 16])
+def test_fused_two_kernel_iteration_matches_three_kernels(tmp_path, k):
+    """The FP32 PCG step as two kernels (the lane apply forms the direction,
+    k_pcg_gather_update does the gather, the vector update and the next
+    step's dots) against the three-kernel step: the same trials to the
+    mixed-precision tolerance and plastic-iteration counts; reruns bitwise."""
+    srfs = [1.0 + 0.02 * t for t in range(k)]
+    env3 = {"SG_APPLY_VARIANT": "3"}
+    a = _variant_trials(0, srfs, tmp_path / "f0.npz", var="SG_FUSED", extra=env3)
+    b = _variant_trials(1, srfs, tmp_path / "f1.npz", var="SG_FUSED", extra=env3)
+    c = _variant_trials(1, srfs, tmp_path / "f1b.npz", var="SG_FUSED", extra=env3)
     assert a["nl"].tolist() == b["nl"].tolist()
     for t in range(k):
         assert rel(b["x"][t], a["x"][t]) <= MIXED_TOL
