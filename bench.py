@@ -7,7 +7,8 @@ synthetic data; a factor-of-safety solve searches SRF on [1, 3] to 0.01 with
 nl_maxiter = 2000.  Form measured: the mixed-precision batched serving form --
 FP32 element matrices and FP32 PCG with FP64 iterative refinement, k = 8
 concurrent SRF trials sharing every element apply as 8 right-hand sides, the
-batch refilled as trials finish (sg_fos with k = 8).
+search is the bisection with its next probes run ahead in the batch (sg_fos with
+k = 8).
 
 A step is one pass of the hot path over one batch: one plastic iteration of
 the 8 trials (FP64-refined linear solve to the reference tolerances, then the
@@ -348,7 +349,7 @@ def precision_vs_oracle(sg, ctx, futures):
 def fos_measured(sg, ctx):
     """Complete factor-of-safety searches on the 576-element cut of the same
     slope (nl_maxiter 2000, SRF on [1, 3] to 0.01): the mixed batched form
-    (k = 8, refilled batch) and the plain FP64 form (bisection, one trial at
+    (k = 8, bisection probes run ahead in the batch) and the plain FP64 form (bisection, one trial at
     a time), each timed end to end, with the plastic iterations each ran."""
     from specfem3d_geotech_gb300 import meshgen
     mesh = meshgen.slope3d(**CUT)
@@ -374,12 +375,36 @@ def fos_measured(sg, ctx):
     return out
 
 
+def admission_report(res, workers, budget):
+    """From each request's timeline: the largest footprint sum that ran at
+    once, and the requests that waited in the queue while a worker was idle
+    (held back by the HBM budget, not by the worker count)."""
+    iv = [(r["t_start"], r["t_done"], r["footprint"]) for r in res]
+    peak = 0.0
+    for t0, _, _ in iv:
+        peak = max(peak, sum(f for a, b, f in iv if a <= t0 < b))
+    held = 0
+    for r in res:
+        a, s = r["t_arrival"], r["t_start"]
+        if s - a < 1e-3:
+            continue
+        # idle worker at some start event inside the wait (other requests' finishes)
+        for _, b, _ in iv:
+            if a <= b < s and sum(1 for x, y, _ in iv if x <= b < y) < workers:
+                held += 1
+                break
+    return {"budget_gb": budget / 1e9, "peak_running_footprint_gb": peak / 1e9,
+            "held_by_budget_with_idle_worker": held}
+
+
 def serving_leg(sg, args):
-    """Config 4 scaled to a bounded run: a seeded Poisson stream of FOS requests
+    """Config 4 as a bounded run: a seeded Poisson stream of FOS requests
     (random slopes, log-uniform mesh sizes, k = 4..16 concurrent trials) through
     the request loop, once in the mixed batched form (4 workers, continuous
-    batching) and once as plain FP64 one at a time (1 worker, bisection, k = 1).
-    Both arms see the same requests and the same nl_maxiter."""
+    batching, admission by estimated HBM footprint within --serve-budget-gb)
+    and once as plain FP64 one at a time (1 worker, bisection, k = 1) on the
+    requests up to --serve-plain-max elements.  Both arms see the same
+    requests and the same nl_maxiter."""
     import numpy as np
     from specfem3d_geotech_gb300 import meshgen
     rng = np.random.default_rng(4)
@@ -388,37 +413,51 @@ def serving_leg(sg, args):
     meshes = [meshgen.random_slope(rng, int(sz)) for sz in sizes]
     ks = rng.integers(4, 17, n)
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, n))
+    budget = int(args.serve_budget_gb * 1e9)
 
-    def run(prec, kof, workers):
+    def run(prec, kof, workers, idx, budget_bytes):
         ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=args.serve_nl, precision=prec)
-        srv = sg.Server(0, 0, workers=workers)
+        srv = sg.Server(0, budget_bytes, workers=workers)
         t0 = time.perf_counter()
         ids = []
-        for i, m in enumerate(meshes):
+        for i in idx:
             dt = arrivals[i] - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
-            ids.append(srv.submit(m, ctl, lo=1.0, hi=3.0, step=0.01, k=kof(i)))
+            ids.append(srv.submit(meshes[i], ctl, lo=1.0, hi=3.0, step=0.01, k=kof(i)))
         res = [srv.wait(r, timeout=7200) for r in ids]
         wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
         lat = [r["t_done"] - r["t_arrival"] for r in res]
-        return res, {"solves_per_s": len(res) / wall, "p50_s": st["p50_s"], "p99_s": st["p99_s"],
-                     "mean_s": float(np.mean(lat)), "peak_concurrent": st["peak_concurrent"],
-                     "trials": int(sum(r["ntrials"] for r in res)), "wall_s": wall,
-                     "ok": all(r["status"] == 0 for r in res)}
+        out = {"requests": len(res), "solves_per_s": len(res) / wall, "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+               "mean_s": float(np.mean(lat)), "peak_concurrent": st["peak_concurrent"],
+               "trials": int(sum(r["ntrials"] for r in res)), "wall_s": wall,
+               "ok": all(r["status"] == 0 for r in res),
+               "admission": admission_report(res, workers, st["budget_bytes"])}
+        return res, out
 
-    rm, mixed = run(sg.PREC_MIXED, lambda i: int(ks[i]), 4)
-    rp, plain = run(sg.PREC_FP64, lambda i: 1, 1)
-    same = sum(1 for a, b in zip(rm, rp) if a["fos"] == b["fos"])
-    return {"requests": n, "rate_per_s": args.serve_rate, "nelmt": [int(r["nelmt"]) for r in rm],
-            "k": [int(k) for k in ks], "nl_maxiter": args.serve_nl,
-            "srf_grid": "k-section (mixed) / bisection (plain) on [1, 3] to 0.01",
-            "mixed_batched": mixed, "plain_fp64_one_at_a_time": plain,
-            "solves_per_s_ratio": mixed["solves_per_s"] / plain["solves_per_s"],
-            "same_critical_srf": f"{same}/{n}", "fos_mixed": [r["fos"] for r in rm],
-            "fos_plain": [r["fos"] for r in rp]}
+    allidx = list(range(n))
+    rm, mixed = run(sg.PREC_MIXED, lambda i: int(ks[i]), 4, allidx, budget)
+    pidx = [i for i in allidx if sizes[i] <= args.serve_plain_max]
+    out = {"requests": n, "rate_per_s": args.serve_rate, "nelmt": [int(r["nelmt"]) for r in rm],
+           "k": [int(k) for k in ks], "nl_maxiter": args.serve_nl,
+           "srf_grid": "bisection on [1, 3] to 0.01 (mixed: k probes run ahead in one batch; plain: one at a time)",
+           "mixed_batched": mixed, "fos_mixed": [r["fos"] for r in rm],
+           "per_request_work": "each trial runs at most nl_maxiter plastic iterations; trials per request in "
+                               "mixed_batched.trials"}
+    if pidx:
+        rp, plain = run(sg.PREC_FP64, lambda i: 1, 1, pidx, 0)
+        sub = [rm[i] for i in pidx]
+        # the same requests in the mixed arm's run: solves/s over that subset's own span
+        same = sum(1 for a, b in zip(sub, rp) if a["fos"] == b["fos"])
+        out["plain_fp64_one_at_a_time"] = plain
+        out["plain_subset"] = f"{len(pidx)} requests of at most {args.serve_plain_max} elements"
+        out["same_critical_srf"] = f"{same}/{len(pidx)}"
+        out["fos_plain"] = [r["fos"] for r in rp]
+        if len(pidx) == n:
+            out["solves_per_s_ratio"] = mixed["solves_per_s"] / plain["solves_per_s"]
+    return out
 
 
 def plain_fp64(sg, ctx, mesh, srf0, args, want_x=False):
@@ -446,6 +485,32 @@ def plain_fp64(sg, ctx, mesh, srf0, args, want_x=False):
     m64.close()
     steps64 = a64["nl_iter"] - b64["nl_iter"]
     return steps64 / (t64 / 1000.0), (a64["cg_tot"] - b64["cg_tot"]) / max(1, steps64), px
+
+
+def excavation_leg(sg, ctx, args):
+    """Config 3 at its full size: the 100 x 100 x 50 = 500k-element block, a
+    20 x 20 m pit removed in 4 lifts of 5 m, overburden initial stress with
+    K0 = 0.5, mixed form (one trial: FP32 operator, FP64 refinement),
+    nl_maxiter bounded by --excavation-nl (the second lift, a 10 m vertical
+    cut in c = 20 kPa, phi = 30 deg soil, is past its critical height and
+    runs to nl_maxiter, as it fails in the reference)."""
+    from specfem3d_geotech_gb300 import meshgen
+    mesh = meshgen.excavation()
+    t0 = time.perf_counter()
+    m = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    t_build = time.perf_counter() - t0
+    ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=args.excavation_nl,
+                          precision=sg.PREC_MIXED)
+    t0 = time.perf_counter()
+    rows = m.excavation(ctl, 1, 50.0, 0.0, 0.5, [2, 3, 4, 5])
+    t_run = time.perf_counter() - t0
+    out = {"mesh": f"excavation 100x100x50 = {m.nelmt} elements, {m.neq} dof", "nl_maxiter": args.excavation_nl,
+           "model_build_s": t_build, "stages_s": t_run, "hbm_bytes": ctx.hbm_used(),
+           "stages": [{"stage": int(r[0]), "inner_pcg_iterations": int(r[1]), "plastic_iterations": int(r[2]),
+                       "uxmax": float(r[3]), "umax": float(r[4]), "fmax": float(r[5]), "failed": int(r[6])}
+                      for r in rows]}
+    m.close()
+    return out
 
 
 def end_to_end(sg, ctx, mesh, srf, k, args, s_mixed, world):
@@ -526,7 +591,7 @@ def run_ours(args, rank, world, local):
         s_plain = fosm["plain_fp64"]["plastic_iterations"]
         count_src = "measured: complete searches on the 576-element cut in this run"
     else:
-        s_mixed = 3 * NL_MAXITER                  # k-section bound: 3 rounds of 8 on 200 steps
+        s_mixed = BISECT_TRIALS * NL_MAXITER      # bound: every bisection decision waits a failure
         s_plain = BISECT_TRIALS * NL_MAXITER
         count_src = "upper bounds: 3 rounds x nl_maxiter (batched), 8 trials x nl_maxiter (bisection)"
     value = world / (s_mixed * step_s)
@@ -562,7 +627,7 @@ def run_ours(args, rank, world, local):
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": workload_config(world, ne, neq, args.nx),
         "form": {"k_trials": k, "step": f"one plastic iteration of the {k}-trial batch",
-                 "search": "sg_fos, k = 8: refilled batch (converged trials raise, failed trials lower the bracket)"},
+                 "search": "sg_fos, k = 8: the bisection with its next probes run ahead in the batch"},
         "fos_plastic_iterations": {"mixed_batched": s_mixed, "plain_fp64": s_plain, "source": count_src},
         "trial_plastic_iters_per_s": rate_all,
         "pcg_iters_per_step": cg / max(1, args.steps),
@@ -588,6 +653,8 @@ def run_ours(args, rank, world, local):
     }
     if rank == 0 and args.serve > 0:
         line["serving"] = serving_leg(sg, args)
+    if rank == 0 and args.excavation:
+        line["excavation_500k"] = excavation_leg(sg, ctx, args)
     if rank == 0 and not args.no_cpu:
         t0 = time.time()
         r = oracle_sample(n_cg=N_CG_REF, iters=CPU_SAMPLE_ITERS)
@@ -619,11 +686,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-fos", action="store_true", help="skip the complete searches on the 576-element cut")
     ap.add_argument("--nx", type=int, default=120, help="elements along x (120 = the 192k-element mesh)")
+    ap.add_argument("--excavation", action="store_true", help="add the 500k-element staged excavation leg")
+    ap.add_argument("--excavation-nl", type=int, default=50, help="nl_maxiter of the excavation leg")
     ap.add_argument("--serve", type=int, default=6, help="requests in the serving leg (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving leg (1/s)")
     ap.add_argument("--serve-min", type=int, default=300, help="smallest request mesh (elements)")
     ap.add_argument("--serve-max", type=int, default=3000, help="largest request mesh (elements)")
     ap.add_argument("--serve-nl", type=int, default=100, help="nl_maxiter of the serving requests")
+    ap.add_argument("--serve-budget-gb", type=float, default=0.0,
+                    help="HBM budget of the mixed server (0 = 90%% of free memory)")
+    ap.add_argument("--serve-plain-max", type=int, default=10 ** 9,
+                    help="largest request (elements) also run by the plain FP64 arm")
     args = ap.parse_args()
     rank, world, local = dist()
     if args.impl == "reference":

@@ -277,15 +277,18 @@ int sg_write_ensight_var(const char* path, const char* description, int ncomp, i
 int sg_srf_sweep(sg_model* model, const sg_control* ctl, int nsrf, const double* srf,
                  sg_trial_result* results, int* ndone);
 
-/* Critical SRF on the grid lo + step*m (m = 0..round((hi-lo)/step)), the
- * smallest grid SRF whose trial fails, assuming lo is stable and hi fails.
- * k = 1 is plain bisection.  k > 1 keeps k trials running as one batch and
- * refills it as results arrive: a converged trial raises the stable bound, a
- * failed one lowers the failing bound, trials outside the bracket are
- * cancelled and free slots take the midpoints of the widest open gaps.  The
- * answer is the bisection's when failure is monotone in SRF.  *ntrials =
- * trials started; *nrounds = bisection steps (k = 1) or result events waited
- * for (k > 1). */
+/* Critical SRF on the grid lo + step*m (m = 0..round((hi-lo)/step)) by
+ * bisection, assuming lo is stable and hi fails (the failure test of the
+ * reference's SRF loop: nl_iter == nl_maxiter, src/slope.F90:441).  k = 1
+ * runs the bisection one trial at a time.  k > 1 runs the same bisection with
+ * its next probes ahead in a batch of k trials: free slots take the
+ * shallowest undecided probes of the current node's subtree, results are
+ * applied in the bisection's own order and probes in the subtree not taken
+ * are cancelled, so the answer is the bisection's for any pattern of
+ * failures.  *ntrials = trials started; *nrounds = bisection steps (k = 1) or
+ * result events waited for (k > 1).  The environment variable
+ * SG_FOS_SEARCH=ksection selects a k-section instead (each result moves the
+ * bracket; the bisection's answer only where failure is monotone in SRF). */
 int sg_fos(sg_model* model, const sg_control* ctl, double lo, double hi, double step, int k,
            double* fos, int* ntrials, int* nrounds);
 /* Plastic iterations run by the model's last sg_fos: batch iterations for

@@ -13,6 +13,7 @@
 #include <array>
 #include <cstring>
 #include <functional>
+#include <map>
 #include <numeric>
 #include <string>
 #include <unordered_map>
@@ -341,6 +342,8 @@ static int pcg_run_t(sg_ctx* C, const Op& op, const PcgBufs<V>& B, int n1, V* u,
     double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (el > 3600.0) { status = SG_ERR_TIMEOUT; C->err = "PCG wall-clock guard"; break; }
   }
+  if constexpr (std::is_same<V, float>::value && (KR == 8 || KR == 16))
+    if (fused) fused_dir_restore<KR>(n1, B.p, B.r, dp, B.cs, s);
   cudaMemcpy(hcs, B.cs, sizeof(ColState) * KR, cudaMemcpyDeviceToHost);
   for (int j = 0; j < kcols; ++j) {
     iters[j] = hcs[j].iters;
@@ -1572,14 +1575,103 @@ static int fos_batched(sg_model* M, const sg_control* ctl, double lo, double ste
   return SG_OK;
 }
 
+// The bisection (k = 1 below) with its next probes run ahead in the batch.
+// The probes of a bisection on [0, Mg] form a fixed tree: node (a, b) probes
+// m = (a + b) / 2 and continues with (a, m) if that trial fails and with
+// (m, b) if it converges.  Every free slot takes the shallowest probe of the
+// current node's subtree that is neither known nor running (breadth first,
+// the lower child first); a result is recorded by grid index, the current
+// node descends as far as the recorded results allow, and the probes outside
+// the new node's interval (the subtree not taken) are cancelled.  The
+// decisions are the bisection's own, in its order, so the answer is the
+// bisection's for any pattern of failures -- also where failure is not
+// monotone in SRF (a trial far above the critical SRF can meet nl_tol once
+// its displacement grows linearly, since uerr then falls like 1/nl_iter).
+// *ntrials = trials started, *nrounds = result events waited for.
+static int fos_speculative(sg_model* M, const sg_control* ctl, int Mg, double lo, double step, int k, int* b_out,
+                           int* ntrials, int* nrounds) {
+  int st = batch_begin_impl(M, ctl, k);
+  if (st != SG_OK) return st;
+  Batch& B = M->B;
+  int a = 0, b = Mg, nt = 0, nr = 0;
+  std::map<int, int> known;          // grid index -> 1 failed, 0 converged
+  std::vector<int> idx(k, -1);       // grid index of each slot's trial, -1 free
+  auto running = [&](int m) {
+    for (int j = 0; j < k; ++j)
+      if (idx[j] == m) return true;
+    return false;
+  };
+  while (true) {
+    while (b - a > 1) {
+      auto it = known.find((a + b) / 2);
+      if (it == known.end()) break;
+      if (it->second) b = (a + b) / 2;
+      else a = (a + b) / 2;
+    }
+    if (b - a <= 1) break;
+    // a running probe strictly inside (a, b) belongs to this node's subtree
+    for (int j = 0; j < k; ++j)
+      if (idx[j] >= 0 && (idx[j] <= a || idx[j] >= b)) {
+        B.slot[j] = Slot();
+        idx[j] = -1;
+      }
+    std::vector<std::pair<int, int>> q = {{a, b}};
+    for (size_t h = 0; h < q.size() && q.size() < 4096; ++h) {
+      int freeslot = -1;
+      for (int j = 0; j < k && freeslot < 0; ++j)
+        if (idx[j] < 0 && !B.slot[j].used) freeslot = j;
+      if (freeslot < 0) break;
+      const int x = q[h].first, y = q[h].second;
+      if (y - x <= 1) continue;
+      const int m = (x + y) / 2;
+      auto it = known.find(m);
+      if (it == known.end() && !running(m)) {
+        int slot = -1;
+        st = batch_add_impl(M, lo + step * m, &slot);
+        if (st != SG_OK) { batch_end_impl(M); return st; }
+        idx[slot] = m;
+        ++nt;
+      }
+      if (it == known.end() || it->second) q.push_back({x, m});
+      if (it == known.end() || !it->second) q.push_back({m, y});
+    }
+    // plastic iterations until at least one probe has finished
+    bool done = false;
+    while (!done) {
+      st = batch_iteration(M);
+      if (st != SG_OK) { batch_end_impl(M); return st; }
+      for (int j = 0; j < k; ++j) done = done || (idx[j] >= 0 && !B.slot[j].live);
+    }
+    ++nr;
+    for (int j = 0; j < k; ++j) {
+      if (idx[j] < 0 || B.slot[j].live) continue;
+      const sg_trial_result& r = B.slot[j].res;
+      if (r.errcode != SG_OK) { batch_end_impl(M); return r.errcode; }
+      known[idx[j]] = r.failed ? 1 : 0;
+      B.slot[j] = Slot();
+      idx[j] = -1;
+    }
+  }
+  batch_end_impl(M);
+  *b_out = b;
+  if (ntrials) *ntrials = nt;
+  if (nrounds) *nrounds = nr;
+  return SG_OK;
+}
+
 int sg_fos(sg_model* M, const sg_control* ctl, double lo, double hi, double step, int k, double* fos, int* ntrials,
            int* nrounds) {
   if (!M || !ctl || step <= 0 || hi <= lo || k < 1 || k > 16 || !fos) return SG_ERR_BADARG;
   const int Mg = (int)std::lround((hi - lo) / step);
   const long long steps0 = M->plastic_steps;
   if (k > 1) {
+    // SG_FOS_SEARCH=ksection: the k-section search (the bisection's answer
+    // only where failure is monotone in SRF); default: the batched bisection
+    const char* e = std::getenv("SG_FOS_SEARCH");
+    const bool ksec = e && std::strcmp(e, "ksection") == 0;
     int b = Mg;
-    int st = fos_batched(M, ctl, lo, step, Mg, k, &b, ntrials, nrounds);
+    int st = ksec ? fos_batched(M, ctl, lo, step, Mg, k, &b, ntrials, nrounds)
+                  : fos_speculative(M, ctl, Mg, lo, step, k, &b, ntrials, nrounds);
     M->fos_steps = M->plastic_steps - steps0;
     if (st != SG_OK) return st;
     *fos = lo + step * b;

@@ -184,6 +184,24 @@ __device__ __forceinline__ bool issue_chunk(const float* __restrict__ Ks, int ne
   return true;
 }
 
+// The element's direction column (lane j): p_old (MODE 0), beta p_old + z
+// (MODE 1), or beta p_old + D (r - alpha kp) with r and kp of the previous
+// step (MODE 2, the fused iteration).
+template <int MODE, int KR>
+__device__ __forceinline__ void gather_dir(float (&p)[NEDOF], const int* idx, bool valid, int j,
+                                           const float* __restrict__ pold, const float* __restrict__ z,
+                                           float beta, float alpha, const FusedDir& fz) {
+#pragma unroll
+  for (int r = 0; r < NEDOF; ++r) {
+    const int gd = valid ? idx[r] : 0;
+    const size_t o = (size_t)gd * KR + j;
+    float pv = pold[o];
+    if constexpr (MODE == 1) pv = fmaf(beta, pv, z[o]);
+    if constexpr (MODE == 2) pv = fmaf(beta, pv, fz.dinv[gd] * fmaf(-alpha, fz.kp[o], fz.r[o]));
+    p[r] = valid ? pv : 0.f;
+  }
+}
+
 template <int KR>
 __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
     const float* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const float* __restrict__ pold,
@@ -224,24 +242,16 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
     const int* idx = ibuf + buf * (S::EPW * IDX) + i * IDX;
     prefetch_indices<KR>(ge, pos, nelmt, ngroups, g + gstride, ibuf + (buf ^ 1) * (S::EPW * IDX), lane);
     float p[NEDOF], y[NEDOF];
-    {
-      const float* pj = pold + j;
-      const float* zj = z + j;
+    // one branch per group, outside the unrolled loops, so that each loop is
+    // a single block whose 81 gathers are all in flight together
+    if (combine == 2)
+      gather_dir<2, KR>(p, idx, valid, j, pold, z, beta, alpha, fz);
+    else if (combine == 1)
+      gather_dir<1, KR>(p, idx, valid, j, pold, z, beta, alpha, fz);
+    else
+      gather_dir<0, KR>(p, idx, valid, j, pold, z, beta, alpha, fz);
 #pragma unroll
-      for (int r = 0; r < NEDOF; ++r) {
-        const int gd = valid ? idx[r] : 0;
-        float pv = pj[(size_t)gd * KR];
-        if (combine == 1) {
-          pv = fmaf(beta, pv, zj[(size_t)gd * KR]);
-        } else if (combine == 2) {
-          // z of this iteration from the previous step: D (r - alpha kp)
-          const float zv = fz.dinv[gd] * fmaf(-alpha, fz.kp[(size_t)gd * KR + j], fz.r[(size_t)gd * KR + j]);
-          pv = fmaf(beta, pv, zv);
-        }
-        p[r] = valid ? pv : 0.f;
-        y[r] = 0.f;
-      }
-    }
+    for (int r = 0; r < NEDOF; ++r) y[r] = 0.f;
     const float* mine = ring + i * CHF;
     auto step = [&](auto cc) {
       constexpr int C = decltype(cc)::value;

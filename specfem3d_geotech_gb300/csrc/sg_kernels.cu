@@ -1033,16 +1033,23 @@ __global__ void __launch_bounds__(RED_THREADS, 4) k_pcg_gather_rows(
 //   q = kp_k   = sum of the row's element products in element order
 //   u += alpha_{k-1} p_{k-1},  r_k = r_{k-1} - alpha_{k-1} kp_{k-1},  z_k = D r_k,
 //   p_k = beta_k p_{k-1} + z_k   (bitwise the p_k of the apply)
-// and the partial sums p_k.q, q.z_k, q.(D q), r_k.r_k and max|p_k|.  The last
-// block stops a column when r_k.r_k <= tol^2 r_0.r_0 (k-1 completed steps);
-// otherwise alpha_k = gamma_k / p_k.q and, without forming r_{k+1},
-//   gamma_{k+1} = r_{k+1}.z_{k+1} = gamma_k - 2 alpha_k q.z_k + alpha_k^2 q.(D q),
+// and the partial sums p_k.q, q.z_k, q.(D q), r_k.r_k, max|p_k| and
+// gamma_k = r_k.z_k.  The last block stops a column when r_k.r_k <= tol^2
+// r_0.r_0 (k-1 completed steps); otherwise alpha_k = gamma_k / p_k.q and,
+// without forming r_{k+1}, one step of the recurrence
+//   gamma_{k+1} = gamma_k - 2 alpha_k q.z_k + alpha_k^2 q.(D q),
 //   beta_{k+1} = gamma_{k+1} / gamma_k.
+// gamma_k itself is summed directly every step: carried from step to step,
+// the recurrence keeps the absolute rounding error of the largest gamma it
+// has seen, which swamps gamma once the FP32 residual has dropped by 1e3
+// (on the layered 3D slope it turned negative within 30 steps).  A single
+// step of it errs by about eps_f32 * sqrt(gamma_k / gamma_{k+1}) relative.
 // So an iteration is two kernels (apply, this) instead of three, and u, r,
 // z and kp make one trip through HBM fewer.  The dots use the compensated
 // FP32 sums of the other kernels; r.r only feeds the stop test and is summed
 // plainly.
-constexpr int GU_NQ = 8;                 // partial quantities per column (5 used)
+constexpr int GU_NQ = 8;                 // partial quantities per column (6 used)
+constexpr int GU_USED = 6;
 constexpr int GU_BLOCKS = 152 * 2;       // two resident CTAs per SM (128 registers)
 
 template <int KR>
@@ -1067,7 +1074,7 @@ __global__ void __launch_bounds__(RED_THREADS, 2) k_pcg_gather_update(
     alpha[k] = (float)cs[j].alpha;
     beta[k] = (float)cs[j].beta;
   }
-  DotAcc<float> sd[4], sa[4], sb[4];
+  DotAcc<float> sd[4], sa[4], sb[4], sg[4];
   float srr[4] = {0.f, 0.f, 0.f, 0.f}, smp[4] = {0.f, 0.f, 0.f, 0.f};
   const float4* yq = reinterpret_cast<const float4*>(Y) + q;
   const int wstride = gridDim.x * GATHER_WARPS * NPW;
@@ -1119,6 +1126,7 @@ __global__ void __launch_bounds__(RED_THREADS, 2) k_pcg_gather_update(
       const float pn = fmaf(beta[k], pa[k], zn);
       sd[k].add(pn, qa[k]);
       sa[k].add(qa[k], zn);
+      sg[k].add(rn, zn);
       sb[k].add(qa[k], dv * qa[k]);
       srr[k] = fmaf(rn, rn, srr[k]);
       smp[k] = fmaxf(smp[k], fabsf(pn));
@@ -1129,18 +1137,18 @@ __global__ void __launch_bounds__(RED_THREADS, 2) k_pcg_gather_update(
     *reinterpret_cast<float4*>(p + o) = make_float4(pa[0], pa[1], pa[2], pa[3]);
     *reinterpret_cast<float4*>(kp + o) = acc;
   }
-  // block partials: [block][column][GU_NQ] = p.q, q.z, q.Dq, r.r, max|p|
-  __shared__ double sred[RED_THREADS / 32][KR][5];
+  // block partials: [block][column][GU_NQ] = p.q, q.z, q.Dq, r.r, max|p|, r.z
+  __shared__ double sred[RED_THREADS / 32][KR][GU_USED];
   auto mine = [&](int k, int qq) -> double {
     if (!(act && live[k])) return 0.0;
     return qq == 0 ? sd[k].value() : qq == 1 ? sa[k].value() : qq == 2 ? sb[k].value()
-                   : qq == 3 ? (double)srr[k] : (double)smp[k];
+                   : qq == 3 ? (double)srr[k] : qq == 4 ? (double)smp[k] : sg[k].value();
   };
 #pragma unroll
   for (int j = 0; j < KR; ++j) {
     const bool own = act && (j >> 2) == (c0 >> 2);
 #pragma unroll
-    for (int qq = 0; qq < 5; ++qq) {
+    for (int qq = 0; qq < GU_USED; ++qq) {
       double v = own ? mine(j & 3, qq) : 0.0;
 #pragma unroll
       for (int o = 16; o >= 1; o >>= 1) {
@@ -1151,8 +1159,8 @@ __global__ void __launch_bounds__(RED_THREADS, 2) k_pcg_gather_update(
     }
   }
   __syncthreads();
-  if (threadIdx.x < KR * 5) {
-    const int j = threadIdx.x / 5, qq = threadIdx.x % 5;
+  if (threadIdx.x < KR * GU_USED) {
+    const int j = threadIdx.x / GU_USED, qq = threadIdx.x % GU_USED;
     double v = 0.0;
     for (int w = 0; w < RED_THREADS / 32; ++w) v = (qq == 4) ? fmax(v, sred[w][j][qq]) : v + sred[w][j][qq];
     part[((size_t)blockIdx.x * KR + j) * GU_NQ + qq] = v;
@@ -1179,22 +1187,27 @@ __global__ void __launch_bounds__(RED_THREADS, 2) k_pcg_gather_update(
     constexpr int NQ = GU_NQ * KR;
     const int jj = threadIdx.x;
     ColState& c = cs[jj];
-    double pq = 0.0, qz = 0.0, qdq = 0.0, rr = 0.0, mp = 0.0;
+    double pq = 0.0, qz = 0.0, qdq = 0.0, rr = 0.0, mp = 0.0, rz = 0.0;
     for (int t = jj * GU_NQ; t < RED_THREADS; t += NQ) {
       pq += sfin[t]; qz += sfin[t + 1]; qdq += sfin[t + 2]; rr += sfin[t + 3]; mp = fmax(mp, sfin[t + 4]);
+      rz += sfin[t + 5];
     }
     if (c.active && !c.done) {
       c.rr = rr;
       if (rr <= c.tol * c.tol * c.rr0) {
-        c.done = 1; c.iters = it - 1;          // alpha and maxp stay those of the last step taken
+        // alpha, maxp and rz (the one-step recurrence value that formed
+        // beta of the direction in p) stay those of the last step taken
+        c.done = 1; c.iters = it - 1;
       } else if (it - 1 >= G->maxiter) {
         c.done = 1; c.failed = 1; c.iters = G->maxiter + 1;
       } else {
-        const double al = c.rz / pq;
-        const double gn = c.rz - 2.0 * al * qz + al * al * qdq;
+        const double al = rz / pq;
+        const double gn = rz - 2.0 * al * qz + al * al * qdq;
         c.alpha = al;
-        c.beta = gn / c.rz;
-        c.rz = gn;
+        // a non-positive one-step value (rounding at the end of a solve)
+        // restarts the direction instead of reversing it
+        c.beta = gn > 0.0 ? gn / rz : 0.0;
+        c.rz = gn > 0.0 ? gn : rz;
         c.maxp = mp;
       }
     }
@@ -1221,6 +1234,32 @@ template void pcg_gather_update<8>(const GatherTopo&, const float*, float*, floa
                                    ColState*, PcgGlobal*, double*, cudaStream_t);
 template void pcg_gather_update<16>(const GatherTopo&, const float*, float*, float*, float*, float*, const float*,
                                     ColState*, PcgGlobal*, double*, cudaStream_t);
+
+// End of a fused solve.  A column that stopped after k steps holds r_k and
+// the direction of step k+1, p_{k+1} = beta_{k+1} p_k + D r_k, with
+// rz = r_k.z_k.  Taking D r_k off leaves beta_{k+1} p_k, so that a solve
+// that continues the direction (keep_dir: p = (r.z_new / rz) p_old + z_new)
+// forms (r.z_new / r_{k-1}.z_{k-1}) p_k + z_new, the continuation of the
+// three-kernel iteration.  Columns that did not take part keep their p.
+template <int KR>
+__global__ void __launch_bounds__(RED_THREADS) k_fused_dir_restore(int n1, float* __restrict__ p,
+                                                                 const float* __restrict__ r,
+                                                                 const float* __restrict__ dinv,
+                                                                 const ColState* __restrict__ cs) {
+  const int j = threadIdx.x & (KR - 1);
+  if (!cs[j].active) return;
+  const size_t n = (size_t)n1 * KR;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    p[i] = p[i] - dinv[i / KR] * r[i];
+}
+
+template <int KR>
+void fused_dir_restore(int n1, float* p, const float* r, const float* dinv, const ColState* cs, cudaStream_t s) {
+  SG_LAUNCH k_fused_dir_restore<KR><<<red_grid((size_t)n1 * KR, RED_THREADS * 4, 152 * 8), RED_THREADS, 0, s>>>(
+      n1, p, r, dinv, cs);
+}
+template void fused_dir_restore<8>(int, float*, const float*, const float*, const ColState*, cudaStream_t);
+template void fused_dir_restore<16>(int, float*, const float*, const float*, const ColState*, cudaStream_t);
 
 bool fused_pcg_enabled() {
   static const bool on = !(getenv("SG_FUSED") && atoi(getenv("SG_FUSED")) == 0);

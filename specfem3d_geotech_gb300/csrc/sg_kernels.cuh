@@ -72,6 +72,10 @@ void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* 
 template <int KR>
 void pcg_gather_update(const GatherTopo& T, const float* Y, float* kp, float* p, float* r, float* u,
                        const float* dinv, ColState* cs, PcgGlobal* G, double* part, cudaStream_t s);
+// After a fused solve: p -= D r for the columns that took part, so that the
+// direction a later keep_dir solve continues is that of the last step taken.
+template <int KR>
+void fused_dir_restore(int n1, float* p, const float* r, const float* dinv, const ColState* cs, cudaStream_t s);
 bool fused_pcg_enabled();   // SG_FUSED=0 keeps the three-kernel iteration
 bool apply_uses_lanes(int dense, int KR);  // the FP32 apply of this operator is k_apply_lanes
 // Matrix-free FP32 apply (sg_apply_mf.cu): rec holds per GLL point J^-1 and the

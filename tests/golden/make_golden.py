@@ -7,6 +7,12 @@ small JSON files instead of being recomputed in every test session.
     python tests/golden/make_golden.py slope2d_sweep     # ~20-40 min, 1 core
     python tests/golden/make_golden.py slope2d_trials    # ~1 min
     python tests/golden/make_golden.py slope3d_cut_fos   # ~1 h, 1 core
+    python tests/golden/make_golden.py deck_trials       # ~5 min, 1 core
+
+tests/golden/decks/ holds two of the reference's own input decks, copied
+unchanged from its input/ folder: validation1 (the slope of its input
+chapter, doc/chap3_input.tex:174-190) and cubit_example (a CUBIT-meshed
+slope with the same material).
 """
 from __future__ import annotations
 
@@ -85,6 +91,30 @@ def slope3d_cut_fos():
     out = dict(mesh="slope3d", cut=SLOPE3D_CUT, nelmt=om.nelmt, neq=om.neq, search="bisection on [1, 3] step 0.01",
                critical_srf=round(lo + step * b, 10), probes=rows, oracle_seconds=time.time() - t0)
     with open(os.path.join(HERE, "slope3d_cut_fos.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+def deck_trials():
+    """The reference's validation1 and cubit_example decks read by the
+    oracle's deck reader: trials at the decks' first three SRFs (1.0, 1.5,
+    2.0) with their summaries and the last two uerr values, so that the GPU
+    runs of the same decks can be compared with the oracle."""
+    out = {}
+    for name in ("validation1", "cubit_example"):
+        om = OracleModel(deck=os.path.join(HERE, "decks", name + ".sem"))
+        rows = []
+        t0 = time.time()
+        for s in (1.0, 1.5, 2.0):
+            r = om.trial(s, want_log=True)
+            ue = r.pop("uerr_log")
+            r.pop("nl_cg")
+            r["uerr_last2"] = [float(v) for v in ue[-2:]]
+            r["seconds"] = time.time() - t0
+            rows.append(r)
+            print(name, json.dumps(r), flush=True)
+        out[name] = dict(nelmt=om.nelmt, neq=om.neq, control={k: (v.tolist() if hasattr(v, "tolist") else v)
+                                                               for k, v in om.control().items()}, trials=rows)
+    with open(os.path.join(HERE, "deck_trials.json"), "w") as f:
         json.dump(out, f, indent=1)
 
 

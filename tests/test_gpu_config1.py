@@ -152,3 +152,23 @@ def test_mixed_batched_trials_match_fp64_oracle(tmp_path, oracle_trials, variant
         assert rel(d["x"][t], ro["x"]) <= MIXED_TOL, (srf, rel(d["x"][t], ro["x"]))
         smax = np.abs(ro["stress"]).max()
         assert np.abs(d["stress"][t] - ro["stress"]).max() <= MIXED_STRESS_TOL * smax
+
+
+def test_factor_of_safety_matches_oracle_bisection(ctx, cut):
+    """The whole search of src/slope.F90:244-443 on the layered 3D cut,
+    nl_maxiter 2000, SRF on [1, 3] to 0.01: the oracle's bisection (the
+    committed record tests/golden/slope3d_cut_fos.json, an hour of CPU) finds
+    1.44; the GPU's plain FP64 bisection finds it with the same probes and
+    failures, and the mixed batched search (k = 8, refilled batch) finds the
+    same critical SRF."""
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "slope3d_cut_fos.json")) as f:
+        gold = json.load(f)
+    mesh = cut[0]
+    m64 = sg.Model(mesh, ctx=ctx)
+    fos64, nt64, _ = m64.fos(sg.make_control(nl_maxiter=2000), 1.0, 3.0, 0.01, k=1)
+    assert abs(fos64 - gold["critical_srf"]) < 1e-9 and nt64 == len(gold["probes"])
+    mx = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
+    fosm, ntm, _ = mx.fos(sg.make_control(nl_maxiter=2000, precision=sg.PREC_MIXED), 1.0, 3.0, 0.01, k=8)
+    assert abs(fosm - gold["critical_srf"]) < 1e-9
+    assert mx.fos_steps() < sum(p["nl_iter"] for p in gold["probes"])

@@ -1,0 +1,76 @@
+"""The reference's own input decks on the GPU.
+
+tests/golden/decks holds two decks copied unchanged from the reference's
+input/ folder: validation1, the slope of its input chapter
+(doc/chap3_input.tex:174-190), and cubit_example, a CUBIT-meshed slope with
+the same soil (gamma 18.8, E 1e5, nu 0.3, phi 20, c 29).  Both are read by the
+product's deck reader (sg_model_from_deck) and run on the device.
+
+* FP64 trials at the decks' SRFs 1.0, 1.5 and 2.0 against the oracle's runs
+  of the same decks (tests/golden/deck_trials.json, made by
+  tests/golden/make_golden.py deck_trials): equal plastic-iteration counts,
+  PCG totals within 1 %, displacement maxima within the trial tolerance.
+* validation1's own SRF list (1.0 1.5 2.0 2.15 ... 2.20) through
+  sg_srf_sweep, the way the reference runs the deck (src/slope.F90:244-443):
+  every listed SRF converges, and the plastic iterations climb through the
+  2.15-2.20 bracket the list was written around (the displacement curve's
+  knee, from which the reference's manual reads the factor of safety).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import specfem3d_geotech_gb300 as sg
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DECKS = os.path.join(HERE, "golden", "decks")
+TRIAL_TOL = 5e-8     # a whole FP64 trial (the oracle's own reordering noise floor is 4e-8)
+
+
+@pytest.fixture(scope="module")
+def oracle_runs():
+    with open(os.path.join(HERE, "golden", "deck_trials.json")) as f:
+        return json.load(f)
+
+
+def _control(m, prec=sg.PREC_FP64):
+    c = m.deck_control()
+    return c, sg.make_control(cg_tol=c["cg_tol"], nl_tol=c["nl_tol"], cg_maxiter=c["cg_maxiter"],
+                              nl_maxiter=c["nl_maxiter"], phinu=c["phinu"], allelastic=c["allelastic"],
+                              precision=prec)
+
+
+@pytest.mark.parametrize("name", ["validation1", "cubit_example"])
+def test_deck_trials_match_oracle(ctx, oracle_runs, name):
+    gold = oracle_runs[name]
+    m = sg.Model(deck=os.path.join(DECKS, name + ".sem"), ctx=ctx)
+    assert (m.nelmt, m.neq) == (gold["nelmt"], gold["neq"])
+    _, ctl = _control(m)
+    for ro in gold["trials"]:
+        r = m.trials([ro["srf"]], ctl)[0]
+        assert r["nl_iter"] == ro["nl_iter"] and r["converged"] == ro["converged"] == 1, (ro["srf"], r, ro)
+        assert abs(r["cg_tot"] - ro["cg_tot"]) <= max(3, 0.01 * ro["cg_tot"]), (r["cg_tot"], ro["cg_tot"])
+        for k in ("umax", "uxmax"):
+            assert abs(r[k] - ro[k]) <= TRIAL_TOL * abs(ro[k]), (k, r[k], ro[k])
+    m.close()
+
+
+def test_validation1_srf_list_sweep(ctx):
+    m = sg.Model(deck=os.path.join(DECKS, "validation1.sem"), ctx=ctx)
+    c, ctl = _control(m)
+    srf = [float(s) for s in c["srf"]]
+    assert srf == [1.0, 1.5, 2.0, 2.15, 2.16, 2.17, 2.18, 2.19, 2.2]
+    res = m.sweep(srf, ctl)
+    assert len(res) == len(srf)
+    assert all(r["converged"] == 1 and r["failed"] == 0 for r in res)
+    nl = [r["nl_iter"] for r in res]
+    um = [r["umax"] for r in res]
+    assert all(b > a for a, b in zip(nl, nl[1:])), nl
+    assert all(b > a for a, b in zip(um, um[1:])), um
+    # the knee: the last step of the list costs several times the first step of the bracket
+    assert nl[-1] > 3 * nl[3], nl
+    m.close()

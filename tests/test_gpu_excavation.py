@@ -13,7 +13,13 @@ against the oracle, on a 6 x 6 x 4 block with a 4 x 4 m pit in 2 m lifts:
   layered 3D slope cut.
 
 Stage rows are [stage, cg_tot, nl_tot, uxmax, umax, fmax, failed, errcode];
-plastic-iteration totals must be equal and displacements within 1e-8.
+plastic-iteration totals and failure flags must be equal, and displacements
+within 1e-8 for stages that converge. A stage that fails has run nl_maxiter
+plastic iterations of a growing mechanism, which amplifies rounding: the
+oracle's own dot-product order variants (sequential, pairwise, strided,
+reverse, 5-way) spread its umax over 0.0518-0.0525 (1.3 %) and its fmax over
+95-112 on the failing stage of the unequal-count case, so failed stages are
+compared at 2e-2.
 """
 import numpy as np
 import pytest
@@ -26,6 +32,7 @@ from specfem3d_geotech_gb300 import meshgen
 pytestmark = pytest.mark.gpu
 
 DISP_TOL = 1e-8
+FAILED_DISP_TOL = 2e-2
 
 
 def _mesh(lifts=2):
@@ -48,7 +55,9 @@ def _same(r, ro):
     assert np.array_equal(r[:, 0], ro[:, 0])
     assert np.array_equal(r[:, 2], ro[:, 2]), (r[:, 2], ro[:, 2])      # plastic iterations per stage
     assert np.array_equal(r[:, 6], ro[:, 6])                           # failed flags
-    assert np.allclose(r[:, 3:5], ro[:, 3:5], rtol=DISP_TOL, atol=0)   # uxmax, umax
+    ok = ro[:, 6] == 0
+    assert np.allclose(r[ok, 3:5], ro[ok, 3:5], rtol=DISP_TOL, atol=0)   # uxmax, umax
+    assert np.allclose(r[~ok, 3:5], ro[~ok, 3:5], rtol=FAILED_DISP_TOL, atol=0)
 
 
 def test_sem_gravity_initial_stress(ctx):
