@@ -267,6 +267,9 @@ def apply_kernel_name(kr: int, nelmt: int) -> str:
     if v == "4" or (v == "5" and nelmt < 100000):
         return f"k_apply_mf<{kr}>"
     if v in ("3", "5") and kr in (8, 16):
+        if os.environ.get("SG_LANE_PAIRS", "0") == "1":
+            mode = 2 if os.environ.get("SG_FUSED", "0") == "1" else 1
+            return f"k_apply_pairs<{kr},{mode}>"
         return f"k_apply_lanes<{kr}>"
     return f"k_apply_sparse_tma<float,{kr}>"
 

@@ -1261,8 +1261,11 @@ void fused_dir_restore(int n1, float* p, const float* r, const float* dinv, cons
 template void fused_dir_restore<8>(int, float*, const float*, const float*, const ColState*, cudaStream_t);
 template void fused_dir_restore<16>(int, float*, const float*, const float*, const ColState*, cudaStream_t);
 
+// Off by default: on the 192k-element slope with 8 trials the fused step took
+// 0.798 + 0.399 ms against 0.717 + 0.231 + 0.207 ms for the three kernels
+// (the apply's direction then gathers r, kp and D besides p).
 bool fused_pcg_enabled() {
-  static const bool on = !(getenv("SG_FUSED") && atoi(getenv("SG_FUSED")) == 0);
+  static const bool on = getenv("SG_FUSED") && atoi(getenv("SG_FUSED")) == 1;
   return on;
 }
 bool apply_uses_lanes(int dense, int KR) { return dense == 0 && (KR == 8 || KR == 16) && g_apply_variant >= 3; }

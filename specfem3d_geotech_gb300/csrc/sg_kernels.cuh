@@ -66,6 +66,15 @@ template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
                         float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
                         FusedDir fz = FusedDir());
+// The lane apply with two warps per element group, each owning half of the
+// element's accumulators (bitwise the same Y); launch_apply_lanes uses it when
+// set_lane_pairs(1) (SG_LANE_PAIRS=1).
+template <int KR>
+void launch_apply_pairs(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
+                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
+                        FusedDir fz);
+extern int g_lane_pairs;
+void set_lane_pairs(int on);
 // Fused FP32 PCG step for 8 or 16 columns (see k_pcg_gather_update): gather
 // of the element products, the previous step's vector update, the new
 // direction and the dots of the next step in one kernel.
@@ -76,7 +85,7 @@ void pcg_gather_update(const GatherTopo& T, const float* Y, float* kp, float* p,
 // direction a later keep_dir solve continues is that of the last step taken.
 template <int KR>
 void fused_dir_restore(int n1, float* p, const float* r, const float* dinv, const ColState* cs, cudaStream_t s);
-bool fused_pcg_enabled();   // SG_FUSED=0 keeps the three-kernel iteration
+bool fused_pcg_enabled();   // SG_FUSED=1 selects the two-kernel iteration
 bool apply_uses_lanes(int dense, int KR);  // the FP32 apply of this operator is k_apply_lanes
 // Matrix-free FP32 apply (sg_apply_mf.cu): rec holds per GLL point J^-1 and the
 // C constants times w detJ; pcg_apply takes it with dense = 2.
