@@ -267,9 +267,6 @@ def apply_kernel_name(kr: int, nelmt: int) -> str:
     if v == "4" or (v == "5" and nelmt < 100000):
         return f"k_apply_mf<{kr}>"
     if v in ("3", "5") and kr in (8, 16):
-        if os.environ.get("SG_LANE_PAIRS", "0") == "1":
-            mode = 2 if os.environ.get("SG_FUSED", "0") == "1" else 1
-            return f"k_apply_pairs<{kr},{mode}>"
         return f"k_apply_lanes<{kr}>"
     return f"k_apply_sparse_tma<float,{kr}>"
 
@@ -349,7 +346,7 @@ def precision_vs_oracle(sg, ctx, futures):
     return out
 
 
-def fos_measured(sg, ctx):
+def fos_measured(sg, ctx, k_mixed=K_TRIALS, extra_ks=()):
     """Complete factor-of-safety searches on the 576-element cut of the same
     slope (nl_maxiter 2000, SRF on [1, 3] to 0.01): the mixed batched form
     (k = 8, bisection probes run ahead in the batch) and the plain FP64 form (bisection, one trial at
@@ -358,7 +355,9 @@ def fos_measured(sg, ctx):
     mesh = meshgen.slope3d(**CUT)
     out = {"mesh": f"slope3d cut {CUT['nx']}x{CUT['ny']}x{CUT['nz']} = {mesh.nelmt} elements",
            "nl_maxiter": NL_MAXITER, "srf_grid": f"[{SRF_LO:g}, {SRF_HI:g}] step {SRF_STEP:g}"}
-    for name, prec, k in (("mixed_batched", sg.PREC_MIXED, K_TRIALS), ("plain_fp64", sg.PREC_FP64, 1)):
+    forms = [("mixed_batched", sg.PREC_MIXED, k_mixed), ("plain_fp64", sg.PREC_FP64, 1)]
+    forms += [(f"mixed_batched_k{kk}", sg.PREC_MIXED, kk) for kk in extra_ks if kk != k_mixed]
+    for name, prec, k in forms:
         m = sg.Model(mesh, precision=prec, ctx=ctx)
         ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=NL_MAXITER, precision=prec)
         t0 = time.perf_counter()
@@ -588,7 +587,7 @@ def run_ours(args, rank, world, local):
     model.close()
 
     # ---- plastic iterations per FOS solve: complete searches on the cut ----
-    fosm = None if args.no_fos else fos_measured(sg, ctx)
+    fosm = None if args.no_fos else fos_measured(sg, ctx, k, [int(v) for v in args.fos_extra_k.split(',') if v])
     if fosm:
         s_mixed = fosm["mixed_batched"]["plastic_iterations"]
         s_plain = fosm["plain_fp64"]["plastic_iterations"]
@@ -688,6 +687,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison and precision report")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-fos", action="store_true", help="skip the complete searches on the 576-element cut")
+    ap.add_argument("--fos-extra-k", default="", help="more batch sizes for the searches on the cut, e.g. 16")
     ap.add_argument("--nx", type=int, default=120, help="elements along x (120 = the 192k-element mesh)")
     ap.add_argument("--excavation", action="store_true", help="add the 500k-element staged excavation leg")
     ap.add_argument("--excavation-nl", type=int, default=50, help="nl_maxiter of the excavation leg")

@@ -417,8 +417,6 @@ sg_ctx* sg_create(int device, size_t hbm_budget) {
   if (const char* v = std::getenv("SG_APPLY_VARIANT")) set_apply_variant(std::atoi(v));
   // SG_GATHER_VARIANT=0 selects the shared-memory-staged gather everywhere.
   if (const char* v = std::getenv("SG_GATHER_VARIANT")) set_gather_variant(std::atoi(v));
-  // SG_LANE_PAIRS=1 runs the lane apply as warp pairs (half the accumulators each).
-  if (const char* v = std::getenv("SG_LANE_PAIRS")) set_lane_pairs(std::atoi(v));
   const KsTables& T = ks_tables();
   c->d_nbr = c->alloc<int>(NGLL * KS_NBR);
   c->d_entry = c->alloc<int>(KS_NNZ);

@@ -300,242 +300,10 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
 
 }  // namespace lanes
 
-// ---------------------------------------------------------------------------
-// Paired-warp form of the lane apply.  Two warps take the same element group:
-// the first owns the accumulators of element nodes 0..13, the second those of
-// nodes 14..26, and each does only the multiply-adds into its own rows.  Both
-// hold all 81 p values, so a lane needs 81 + 42 registers instead of 81 + 81
-// and an SM runs 12 warps instead of 8: the lane apply is latency-bound (2
-// warps per sub-partition leave issue idle about 70 % of cycles), and the
-// pair costs only a second stream of the group's element matrices from L2
-// and a second p gather.  Each accumulator receives the same products in the
-// same storage order as in the one-warp form, so Y is bitwise the same.
-// Chunks: 12 of 204 floats, a 3-stage ring per warp (4 phases per stage and
-// group, so stage and parity stay compile-time constants).
-namespace pairs {
-
-using lanes::BT;
-constexpr int NWP = 6;                 // warp pairs per CTA, one CTA per SM
-constexpr int NW = 2 * NWP;
-constexpr int CHF = 204;               // floats per chunk slot (51 float4, 816 B: distinct bank groups)
-constexpr int NCH = 12;                // 11 x 204 + 188 = KS_STRIDE
-constexpr int NSTAGE = 3;
-constexpr int LAST_F4 = (KS_STRIDE - (NCH - 1) * CHF) / 4;
-constexpr int SPLIT = 14;              // first node of the second warp's half
-static_assert((NCH - 1) * CHF < KS_STRIDE && NCH * CHF >= KS_STRIDE, "chunking");
-static_assert(NCH % NSTAGE == 0 && (NCH / NSTAGE) % 2 == 0, "static stage and parity");
-static_assert((KS_STRIDE - (NCH - 1) * CHF) % 4 == 0 && CHF % 4 == 0, "16-byte chunk copies");
-
-template <int H>
-struct Half {
-  static constexpr int N0 = H == 0 ? 0 : SPLIT;
-  static constexpr int N1 = H == 0 ? SPLIT : NGLL;
-  static constexpr int NY = 3 * (N1 - N0);
-  static constexpr bool own(int n) { return n >= N0 && n < N1; }
-};
-
-template <int H, int T>
-constexpr bool needed() {
-  if (T >= KS_NNZ) return false;
-  return Half<H>::own(BT.n[T / 9]) || Half<H>::own(BT.m[T / 9]);
-}
-
-template <int H, int T>
-__device__ __forceinline__ void entry(float v, const float (&p)[NEDOF], float (&y)[Half<H>::NY]) {
-  if constexpr (T < KS_NNZ) {
-    constexpr int b = T / 9, c = (T % 9) / 3, d = T % 3;
-    constexpr int n = BT.n[b], m = BT.m[b], o = Half<H>::N0;
-    if constexpr (Half<H>::own(n)) y[3 * (n - o) + c] = fmaf(v, p[3 * m + d], y[3 * (n - o) + c]);
-    if constexpr (n != m && Half<H>::own(m)) y[3 * (m - o) + d] = fmaf(v, p[3 * n + c], y[3 * (m - o) + d]);
-  }
-}
-
-template <int H, int C, int... F>
-__device__ __forceinline__ void chunk_entries(const float4* __restrict__ src, const float (&p)[NEDOF],
-                                              float (&y)[Half<H>::NY], std::integer_sequence<int, F...>) {
-  (
-      [&] {
-        constexpr int T = C * CHF + 4 * F;
-        if constexpr (needed<H, T>() || needed<H, T + 1>() || needed<H, T + 2>() || needed<H, T + 3>()) {
-          const float4 v = src[F];
-          entry<H, T + 0>(v.x, p, y);
-          entry<H, T + 1>(v.y, p, y);
-          entry<H, T + 2>(v.z, p, y);
-          entry<H, T + 3>(v.w, p, y);
-        }
-      }(),
-      ...);
-}
-
-constexpr unsigned chunk_bytes(int c) { return (unsigned)(c == NCH - 1 ? LAST_F4 * 16 : CHF * 4); }
-
-template <int KR>
-struct Shape {
-  static constexpr int EPW = 32 / KR;
-  static constexpr int STAGE_F = EPW * CHF;
-  static constexpr int RING_F = NSTAGE * STAGE_F;
-  static constexpr int IBUF = 2 * EPW * lanes::IDX;
-  static constexpr int BAR_BYTES = 512;
-  static constexpr size_t SMEM = BAR_BYTES + (size_t)NW * RING_F * 4 + (size_t)NW * IBUF * 4;
-};
-static_assert(Shape<8>::SMEM <= 227 * 1024, "shared memory of one CTA");
-
-template <int KR>
-__device__ __forceinline__ bool issue_chunk(const float* __restrict__ Ks, int nelmt, int ngroups, int g, int c,
-                                            float* ring, uint64_t* bar) {
-  using S = Shape<KR>;
-  if (g >= ngroups) return false;
-  const int e0 = g * S::EPW;
-  const int nv = min(S::EPW, nelmt - e0);
-  const unsigned bytes = chunk_bytes(c);
-  float* dst = ring + (c % NSTAGE) * S::STAGE_F;
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  lanes::expect_tx(bar + (c % NSTAGE), bytes * (unsigned)nv);
-  for (int i = 0; i < nv; ++i)
-    lanes::bulk_copy(dst + i * CHF, Ks + (size_t)(e0 + i) * KS_STRIDE + (size_t)c * CHF, bytes, bar + (c % NSTAGE));
-  return true;
-}
-
-template <int KR, int MODE, int H>
-__device__ __forceinline__ void run(const float* __restrict__ Ks, const int* __restrict__ ge, int nelmt,
-                                    const float* __restrict__ pold, const float* __restrict__ z,
-                                    float* __restrict__ Y, const ColState* __restrict__ cs,
-                                    const int* __restrict__ pos, int* __restrict__ err, const FusedDir& fz,
-                                    uint64_t* bar, float* ring, int* ibuf, int g, int gstride) {
-  using S = Shape<KR>;
-  const int lane = threadIdx.x & 31;
-  const int i = lane / KR, j = lane % KR;
-  const int ngroups = (nelmt + S::EPW - 1) / S::EPW;
-  const float beta = MODE ? (float)cs[j].beta : 0.f;
-  const float alpha = MODE == 2 ? (float)cs[j].alpha : 0.f;
-  int issued = 0, waited = 0;
-  if (lane == 0)
-    for (int c = 0; c < NSTAGE - 1; ++c) issued += issue_chunk<KR>(Ks, nelmt, ngroups, g, c, ring, bar);
-  issued = __shfl_sync(0xffffffffu, issued, 0);
-  lanes::prefetch_indices<KR>(ge, pos, nelmt, ngroups, g, ibuf, lane);
-  bool ok = true;
-  for (int buf = 0; g < ngroups && ok; g += gstride, buf ^= 1) {
-    const int e = g * S::EPW + i;
-    const bool valid = e < nelmt;
-    lanes::cp_async_wait_all();
-    __syncwarp();
-    const int* idx = ibuf + buf * (S::EPW * lanes::IDX) + i * lanes::IDX;
-    lanes::prefetch_indices<KR>(ge, pos, nelmt, ngroups, g + gstride, ibuf + (buf ^ 1) * (S::EPW * lanes::IDX), lane);
-    float p[NEDOF], y[Half<H>::NY];
-    lanes::gather_dir<MODE, KR>(p, idx, valid, j, pold, z, beta, alpha, fz);
-#pragma unroll
-    for (int r = 0; r < Half<H>::NY; ++r) y[r] = 0.f;
-    const float* mine = ring + i * CHF;
-    auto step = [&](auto cc) {
-      constexpr int C = decltype(cc)::value;
-      if (!ok) return;
-      if (lane == 0) {
-        constexpr int CN = C + NSTAGE - 1;
-        issued += (CN < NCH) ? issue_chunk<KR>(Ks, nelmt, ngroups, g, CN, ring, bar)
-                             : issue_chunk<KR>(Ks, nelmt, ngroups, g + gstride, CN - NCH, ring, bar);
-      }
-      const bool w = __all_sync(0xffffffffu, lanes::mbar_wait(bar + (C % NSTAGE), (unsigned)((C / NSTAGE) & 1)));
-      if (!w) {
-        if (lane == 0) atomicExch(err, 1);
-        ok = false;
-        return;
-      }
-      ++waited;
-      const float4* src = reinterpret_cast<const float4*>(mine + (C % NSTAGE) * S::STAGE_F);
-      chunk_entries<H, C>(src, p, y, std::make_integer_sequence<int, (C == NCH - 1) ? LAST_F4 : CHF / 4>{});
-      __syncwarp();
-    };
-    lanes::for_chunks(step, std::make_integer_sequence<int, NCH>{});
-    if (!ok) break;
-    if (valid) {
-#pragma unroll
-      for (int a = Half<H>::N0; a < Half<H>::N1; ++a) {
-        const int q = idx[NEDOF + a];
-        if (q >= 0) {
-          float* dst = Y + (size_t)q * 3 * KR + j;
-          const int o = 3 * (a - Half<H>::N0);
-          dst[0] = y[o];
-          dst[KR] = y[o + 1];
-          dst[2 * KR] = y[o + 2];
-        }
-      }
-    }
-  }
-  lanes::cp_async_wait_all();
-  issued = __shfl_sync(0xffffffffu, issued, 0);
-  for (int q = waited; q < issued; ++q)
-    lanes::mbar_wait(bar + (q % NCH) % NSTAGE, (unsigned)(((q % NCH) / NSTAGE) & 1));
-}
-
-template <int KR, int MODE>
-__global__ void __launch_bounds__(NW * 32, 1) k_apply_pairs(
-    const float* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const float* __restrict__ pold,
-    const float* __restrict__ z, float* __restrict__ Y, const ColState* __restrict__ cs,
-    const PcgGlobal* __restrict__ G, const int* __restrict__ pos, int* __restrict__ err, FusedDir fz) {
-  using S = Shape<KR>;
-  if (G && G->all_done) return;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem) + warp * NSTAGE;
-  float* ring = reinterpret_cast<float*>(smem + S::BAR_BYTES) + (size_t)warp * S::RING_F;
-  int* ibuf = reinterpret_cast<int*>(smem + S::BAR_BYTES + (size_t)NW * S::RING_F * 4) + (size_t)warp * S::IBUF;
-  if (lane == 0) {
-    for (int s = 0; s < NSTAGE; ++s) lanes::mbar_init(bar + s, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  const int g = blockIdx.x * NWP + (warp >> 1), gstride = gridDim.x * NWP;
-  if (warp & 1)
-    run<KR, MODE, 1>(Ks, ge, nelmt, pold, z, Y, cs, pos, err, fz, bar, ring, ibuf, g, gstride);
-  else
-    run<KR, MODE, 0>(Ks, ge, nelmt, pold, z, Y, cs, pos, err, fz, bar, ring, ibuf, g, gstride);
-}
-
-template <int KR, int MODE>
-void launch(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, float* Y,
-            const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s, FusedDir fz) {
-  using S = Shape<KR>;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_apply_pairs<KR, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
-    attr = true;
-  }
-  const int ngroups = (nelmt + S::EPW - 1) / S::EPW;
-  const int ctas = (ngroups + NWP - 1) / NWP;
-  const int grid = ctas < 152 ? ctas : 152;
-  if (grid < 1) return;
-  k_apply_pairs<KR, MODE><<<grid, NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, Y, cs, G, pos, err, fz);
-}
-
-}  // namespace pairs
-
-int g_lane_pairs = 0;
-void set_lane_pairs(int on) { g_lane_pairs = on; }
-
-template <int KR>
-void launch_apply_pairs(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
-                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
-                        FusedDir fz) {
-  if (combine == 2)
-    pairs::launch<KR, 2>(Ks, ge, nelmt, pold, z, Y, cs, G, pos, err, s, fz);
-  else if (combine == 1)
-    pairs::launch<KR, 1>(Ks, ge, nelmt, pold, z, Y, cs, G, pos, err, s, fz);
-  else
-    pairs::launch<KR, 0>(Ks, ge, nelmt, pold, z, Y, cs, G, pos, err, s, fz);
-}
-template void launch_apply_pairs<8>(const float*, const int*, int, const float*, const float*, int, float*,
-                                    const ColState*, const PcgGlobal*, const int*, int*, cudaStream_t, FusedDir);
-template void launch_apply_pairs<16>(const float*, const int*, int, const float*, const float*, int, float*,
-                                     const ColState*, const PcgGlobal*, const int*, int*, cudaStream_t, FusedDir);
-
 template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
                         float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
                         FusedDir fz) {
-  if (g_lane_pairs) {
-    launch_apply_pairs<KR>(Ks, ge, nelmt, pold, z, combine, Y, cs, G, pos, err, s, fz);
-    return;
-  }
   using S = lanes::Shape<KR>;
   static bool attr = false;
   if (!attr) {

@@ -66,15 +66,6 @@ template <int KR>
 void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
                         float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
                         FusedDir fz = FusedDir());
-// The lane apply with two warps per element group, each owning half of the
-// element's accumulators (bitwise the same Y); launch_apply_lanes uses it when
-// set_lane_pairs(1) (SG_LANE_PAIRS=1).
-template <int KR>
-void launch_apply_pairs(const float* Ks, const int* ge, int nelmt, const float* pold, const float* z, int combine,
-                        float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
-                        FusedDir fz);
-extern int g_lane_pairs;
-void set_lane_pairs(int on);
 // Fused FP32 PCG step for 8 or 16 columns (see k_pcg_gather_update): gather
 // of the element products, the previous step's vector update, the new
 // direction and the dots of the next step in one kernel.

@@ -350,19 +350,6 @@ def test_fused_two_kernel_iteration_matches_three_kernels(tmp_path, k):
     assert np.array_equal(b["x"], c["x"]) and np.array_equal(b["cg"], c["cg"])
 
 
-@pytest.mark.parametrize("k", [8, 16])
-def test_paired_lane_apply_bitwise_equals_lane_apply(tmp_path, k):
-    """The lane apply as warp pairs (each warp owns half of an element's
-    accumulators and adds the same products in the same storage order): the
-    same trials bit for bit, in the three-kernel and the fused iteration."""
-    srfs = [1.0 + 0.02 * t for t in range(k)]
-    for fused in ("0", "1"):
-        env = {"SG_APPLY_VARIANT": "3", "SG_FUSED": fused}
-        a = _variant_trials(0, srfs, tmp_path / f"l{fused}.npz", var="SG_LANE_PAIRS", extra=env)
-        b = _variant_trials(1, srfs, tmp_path / f"p{fused}.npz", var="SG_LANE_PAIRS", extra=env)
-        assert np.array_equal(a["x"], b["x"]) and np.array_equal(a["cg"], b["cg"]) and np.array_equal(a["nl"], b["nl"])
-
-
 def test_row_gather_matches_staged_gather(tmp_path):
     """The row-cooperative FP32 gather (coalesced 16-byte pieces, no shared
     memory) gives the staged gather's trials to the mixed-precision tolerance
