@@ -507,7 +507,7 @@ def excavation_leg(sg, ctx, args):
     rows = m.excavation(ctl, 1, 50.0, 0.0, 0.5, [2, 3, 4, 5])
     t_run = time.perf_counter() - t0
     out = {"mesh": f"excavation 100x100x50 = {m.nelmt} elements, {m.neq} dof", "nl_maxiter": args.excavation_nl,
-           "model_build_s": t_build, "stages_s": t_run, "hbm_bytes": ctx.hbm_used(),
+           "model_build_s": t_build, "stages_s": t_run, "hbm_bytes": ctx.hbm_used,
            "stages": [{"stage": int(r[0]), "inner_pcg_iterations": int(r[1]), "plastic_iterations": int(r[2]),
                        "uxmax": float(r[3]), "umax": float(r[4]), "fmax": float(r[5]), "failed": int(r[6])}
                       for r in rows]}

@@ -186,26 +186,35 @@ __device__ __forceinline__ bool issue_chunk(const float* __restrict__ Ks, int ne
 
 // The element's direction column (lane j): p_old (MODE 0), beta p_old + z
 // (MODE 1), or beta p_old + D (r - alpha kp) with r and kp of the previous
-// step (MODE 2, the fused iteration).
+// step (MODE 2, the fused iteration).  Every gather is issued before any is
+// combined: the second operand lands in t, the element's accumulators, which
+// are free until the products start (and are zeroed here), so all 162 loads
+// of a lane are in flight together without registers of their own.
 template <int MODE, int KR>
-__device__ __forceinline__ void gather_dir(float (&p)[NEDOF], const int* idx, bool valid, int j,
+__device__ __forceinline__ void gather_dir(float (&p)[NEDOF], float (&t)[NEDOF], const int* idx, bool valid, int j,
                                            const float* __restrict__ pold, const float* __restrict__ z,
                                            float beta, float alpha, const FusedDir& fz) {
 #pragma unroll
   for (int r = 0; r < NEDOF; ++r) {
     const int gd = valid ? idx[r] : 0;
     const size_t o = (size_t)gd * KR + j;
-    float pv = pold[o];
-    if constexpr (MODE == 1) pv = fmaf(beta, pv, z[o]);
-    if constexpr (MODE == 2) pv = fmaf(beta, pv, fz.dinv[gd] * fmaf(-alpha, fz.kp[o], fz.r[o]));
+    p[r] = pold[o];
+    if constexpr (MODE == 1) t[r] = z[o];
+    if constexpr (MODE == 2) t[r] = fz.dinv[gd] * fmaf(-alpha, fz.kp[o], fz.r[o]);
+  }
+#pragma unroll
+  for (int r = 0; r < NEDOF; ++r) {
+    float pv = p[r];
+    if constexpr (MODE != 0) pv = fmaf(beta, pv, t[r]);
     p[r] = valid ? pv : 0.f;
+    t[r] = 0.f;
   }
 }
 
-template <int KR>
+template <int KR, int MODE>
 __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
     const float* __restrict__ Ks, const int* __restrict__ ge, int nelmt, const float* __restrict__ pold,
-    const float* __restrict__ z, int combine, float* __restrict__ Y, const ColState* __restrict__ cs,
+    const float* __restrict__ z, float* __restrict__ Y, const ColState* __restrict__ cs,
     const PcgGlobal* __restrict__ G, const int* __restrict__ pos, int* __restrict__ err, FusedDir fz) {
   using S = Shape<KR>;
   if (G && G->all_done) return;
@@ -223,8 +232,8 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  const float beta = combine ? (float)cs[j].beta : 0.f;
-  const float alpha = combine == 2 ? (float)cs[j].alpha : 0.f;
+  const float beta = MODE ? (float)cs[j].beta : 0.f;
+  const float alpha = MODE == 2 ? (float)cs[j].alpha : 0.f;
   // chunks issued / waited, counted along the warp's chunk sequence
   int issued = 0, waited = 0;
   if (lane == 0)
@@ -242,16 +251,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_apply_lanes(
     const int* idx = ibuf + buf * (S::EPW * IDX) + i * IDX;
     prefetch_indices<KR>(ge, pos, nelmt, ngroups, g + gstride, ibuf + (buf ^ 1) * (S::EPW * IDX), lane);
     float p[NEDOF], y[NEDOF];
-    // one branch per group, outside the unrolled loops, so that each loop is
-    // a single block whose 81 gathers are all in flight together
-    if (combine == 2)
-      gather_dir<2, KR>(p, idx, valid, j, pold, z, beta, alpha, fz);
-    else if (combine == 1)
-      gather_dir<1, KR>(p, idx, valid, j, pold, z, beta, alpha, fz);
-    else
-      gather_dir<0, KR>(p, idx, valid, j, pold, z, beta, alpha, fz);
-#pragma unroll
-    for (int r = 0; r < NEDOF; ++r) y[r] = 0.f;
+    gather_dir<MODE, KR>(p, y, idx, valid, j, pold, z, beta, alpha, fz);
     const float* mine = ring + i * CHF;
     auto step = [&](auto cc) {
       constexpr int C = decltype(cc)::value;
@@ -305,16 +305,24 @@ void launch_apply_lanes(const float* Ks, const int* ge, int nelmt, const float* 
                         float* Y, const ColState* cs, const PcgGlobal* G, const int* pos, int* err, cudaStream_t s,
                         FusedDir fz) {
   using S = lanes::Shape<KR>;
+  // one kernel per way of forming the direction (separate register budgets)
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(lanes::k_apply_lanes<KR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    cudaFuncSetAttribute(lanes::k_apply_lanes<KR, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    cudaFuncSetAttribute(lanes::k_apply_lanes<KR, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
+    cudaFuncSetAttribute(lanes::k_apply_lanes<KR, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::SMEM);
     attr = true;
   }
   const int ngroups = (nelmt + S::EPW - 1) / S::EPW;
   const int warps = (ngroups + lanes::NW - 1) / lanes::NW;
   int grid = warps < 152 ? warps : 152;
   if (grid < 1) return;
-  lanes::k_apply_lanes<KR><<<grid, lanes::NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, combine, Y, cs, G, pos, err, fz);
+  if (combine == 2)
+    lanes::k_apply_lanes<KR, 2><<<grid, lanes::NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, Y, cs, G, pos, err, fz);
+  else if (combine == 1)
+    lanes::k_apply_lanes<KR, 1><<<grid, lanes::NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, Y, cs, G, pos, err, fz);
+  else
+    lanes::k_apply_lanes<KR, 0><<<grid, lanes::NW * 32, S::SMEM, s>>>(Ks, ge, nelmt, pold, z, Y, cs, G, pos, err, fz);
 }
 
 size_t apply_lanes_smem(int KR) {
