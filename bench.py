@@ -534,6 +534,55 @@ def end_to_end(sg, ctx, mesh, srf, k, args, s_mixed, world):
             "includes": "mesh upload, device model build (stiffness), cold-start plastic iterations, x download"}
 
 
+def _oracle_sweep_worker(q):
+    from oracle.pyoracle import OracleModel
+    from specfem3d_geotech_gb300 import meshgen
+    m = meshgen.slope2d()
+    om = OracleModel(m)
+    t0 = time.perf_counter()
+    rows = om.sweep(list(m.control.srf))
+    q.put({"seconds": time.perf_counter() - t0, "trials": len(rows),
+           "plastic_iterations": int(sum(r["nl_iter"] for r in rows)),
+           "critical_srf": next((r["srf"] for r in rows if r["failed"]), None)})
+
+
+def run_config0(args, rank):
+    """The reference's own CPU-sized case (the 300-element plane-strain slope,
+    SRF 1.00, 1.05, ... until the first failure, nl_maxiter 2000): the whole
+    sweep timed on the GPU (FP64, the drop-in path) and by the oracle on one
+    host core, started together (the oracle in a spawned process)."""
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    ctxp = mp.get_context("spawn")
+    q = ctxp.Queue()
+    proc = ctxp.Process(target=_oracle_sweep_worker, args=(q,))
+    proc.start()
+    import specfem3d_geotech_gb300 as sg
+    from specfem3d_geotech_gb300 import build, meshgen
+    build.build()
+    ctx = sg.Context(0)
+    mesh = meshgen.slope2d()
+    m = sg.Model(mesh, ctx=ctx)
+    c = mesh.control
+    ctl = sg.make_control(cg_tol=c.cg_tol, nl_tol=c.nl_tol, cg_maxiter=c.cg_maxiter, nl_maxiter=c.nl_maxiter)
+    t0 = time.perf_counter()
+    rows = m.sweep(list(c.srf), ctl)
+    t_gpu = time.perf_counter() - t0
+    m.close()
+    cpu = q.get(timeout=3600)
+    proc.join()
+    out = {"config0_sweep": {
+        "case": "300-element plane-strain slope (30x1x10 hex, NGLL=3), SRF 1.00:0.05 to the first failure, "
+                "nl_maxiter 2000, FP64",
+        "gpu_fp64": {"seconds": t_gpu, "trials": len(rows), "plastic_iterations": int(sum(r["nl_iter"] for r in rows)),
+                     "critical_srf": next((r["srf"] for r in rows if r["failed"]), None)},
+        "cpu_oracle_1core": cpu, "speedup": cpu["seconds"] / t_gpu}}
+    print(json.dumps(out), flush=True)
+    ctx.close()
+    return 0
+
+
 def run_ours(args, rank, world, local):
     import numpy as np
     # oracle trials for the precision report start before any GPU call
@@ -690,6 +739,8 @@ def main():
     ap.add_argument("--fos-extra-k", default="", help="more batch sizes for the searches on the cut, e.g. 16")
     ap.add_argument("--nx", type=int, default=120, help="elements along x (120 = the 192k-element mesh)")
     ap.add_argument("--excavation", action="store_true", help="add the 500k-element staged excavation leg")
+    ap.add_argument("--config0", action="store_true",
+                    help="only time the 300-element slope's SRF sweep on the GPU and by the oracle on one core")
     ap.add_argument("--excavation-nl", type=int, default=50, help="nl_maxiter of the excavation leg")
     ap.add_argument("--serve", type=int, default=6, help="requests in the serving leg (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate of the serving leg (1/s)")
@@ -704,6 +755,8 @@ def main():
     rank, world, local = dist()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.config0:
+        return run_config0(args, rank)
     return run_ours(args, rank, world, local)
 
 
