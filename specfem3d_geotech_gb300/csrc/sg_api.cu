@@ -1497,8 +1497,9 @@ int sg_srf_sweep(sg_model* M, const sg_control* ctl, int nsrf, const double* srf
 // trial fails (the failure test of src/slope.F90:441, nl_iter == nl_maxiter),
 // assuming lo is stable and hi fails, as a bisection does.
 //
-// k = 1: bisection, one trial at a time.
-// k > 1: a continuously refilled batch of k trials.  A trial that converges
+// k = 1: bisection, one trial at a time (sg_fos).
+// k > 1 here: the k-section kept behind SG_FOS_SEARCH=ksection (sg_fos runs
+// fos_speculative by default), a continuously refilled batch of k trials.  A trial that converges
 // raises the stable bound a, one that fails lowers the failing bound b, and
 // every running trial outside (a, b) is cancelled; each free slot takes the
 // midpoint of the widest open gap between a, the running probes and b (gaps
@@ -1506,8 +1507,8 @@ int sg_srf_sweep(sg_model* M, const sg_control* ctl, int nsrf, const double* srf
 // converges).  Converging trials report after tens to hundreds of plastic
 // iterations while failing ones take nl_maxiter, so the bracket closes from
 // below while the failures are still running, and the search needs about
-// two failure waits instead of one per k-section round.  Under the same
-// monotonicity the answer is the bisection's.
+// two failure waits instead of one per k-section round.  Only where failure
+// is monotone in SRF is the answer the bisection's.
 // *ntrials = trials started, *nrounds = result events the search waited for.
 static int fos_batched(sg_model* M, const sg_control* ctl, double lo, double step, int Mg, int k, int* b_out,
                        int* ntrials, int* nrounds) {

@@ -6,7 +6,7 @@
 // order when their HBM footprint fits the server's budget.  Each worker thread owns a context (its own CUDA stream),
 // so admitted requests run concurrently and their kernels overlap on the
 // device; inside a request the SRF trials run as a continuously refilled
-// batch (sg_fos: k probes per k-section round share every element apply).
+// batch (sg_fos: the bisection's next k probes share every element apply).
 // A finished request releases its memory, which admits the next ones.
 #include <algorithm>
 #include <chrono>
