@@ -48,10 +48,24 @@ NL_MAXITER = 2000
 SRF_LO, SRF_HI, SRF_STEP = 1.0, 3.0, 0.01
 GRID = int(round((SRF_HI - SRF_LO) / SRF_STEP))
 BISECT_TRIALS = math.ceil(math.log2(GRID))   # 8 trials of a bisection on the 200-step grid
-# FP64 PCG iterations per plastic iteration of the reference algorithm on the
-# 192k mesh (the plain FP64 leg of this benchmark measures 802.9 at the
-# benchmark's SRF); both arms scale the CPU sample with this one number.
-N_CG_REF = 803
+GOLDEN_PCG = os.path.join(ROOT, "tests", "golden", "slope3d_192k_pcg.json")
+
+
+def pcg_count_ref():
+    """FP64 PCG iterations per plastic iteration of the reference algorithm on
+    the 192k mesh at the SRF of the benchmark's first trial: the oracle's own
+    count on that mesh (warm-started plastic iterations after the first,
+    tests/golden/slope3d_192k_pcg.json), else the plain FP64 GPU leg's count
+    from an earlier run.  Both CPU arms scale their timed sample with it."""
+    try:
+        with open(GOLDEN_PCG) as f:
+            g = json.load(f)
+        return float(g["pcg_steady"]), "oracle on the 192k mesh (tests/golden/slope3d_192k_pcg.json)"
+    except Exception:
+        return 861.5, "plain FP64 GPU leg on the 192k mesh"
+
+
+N_CG_REF, N_CG_SRC = pcg_count_ref()
 K_TRIALS = 8
 CPU_SAMPLE_ITERS = 200       # PCG iterations of the oracle's timed sample (about 10 s of CPU work)
 CUT = dict(nx=24, ny=4, nz=6)   # the 576-element cut of the benchmark slope
@@ -243,7 +257,7 @@ def run_reference(args, rank, world):
     value = rate / s_ref
     sample = (f"oracle (serial FP64 restatement of the reference path) on a 6,000-element cut of the same slope "
               f"(120x5x10): 30 PCG iterations + 1 stress pass per process, scaled by element count to 192k "
-              f"elements and to {N_CG_REF} PCG iterations per plastic iteration; {procs} independent processes "
+              f"elements and to {N_CG_REF:g} PCG iterations per plastic iteration ({N_CG_SRC}); {procs} independent processes "
               f"(independent trials); {s_ref} trial plastic iterations per FOS solve ({s_src})")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
@@ -715,7 +729,7 @@ def run_ours(args, rank, world, local):
             "value": cpu_rate / s_ref, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": (f"oracle on a 6,000-element cut of the same slope ({CPU_SAMPLE_ITERS} PCG iterations + "
                        f"1 stress pass, {time.time() - t0:.0f} s), scaled by element count to 192k elements and to "
-                       f"{N_CG_REF} PCG iterations per plastic iteration; {s_ref} trial plastic iterations per "
+                       f"{N_CG_REF:g} PCG iterations per plastic iteration ({N_CG_SRC}); {s_ref} trial plastic iterations per "
                        f"FOS solve ({s_src})")}
     if oex is not None:
         oex.shutdown(wait=False, cancel_futures=True)
