@@ -441,7 +441,13 @@ def serving_leg(sg, args):
             if dt > 0:
                 time.sleep(dt)
             ids.append(srv.submit(meshes[i], ctl, lo=1.0, hi=3.0, step=0.01, k=kof(i)))
-        res = [srv.wait(r, timeout=7200) for r in ids]
+        res = []
+        for i, r in zip(idx, ids):
+            res.append(srv.wait(r, timeout=7200))
+            # progress on stderr, so that a run cut short still leaves its finished requests
+            print(json.dumps({"serving_request": i, "prec": int(prec), **{kk: res[-1][kk] for kk in (
+                "nelmt", "fos", "ntrials", "status", "footprint", "t_arrival", "t_start", "t_done")}}),
+                  file=sys.stderr, flush=True)
         wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
