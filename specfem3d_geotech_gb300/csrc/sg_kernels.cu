@@ -1159,10 +1159,13 @@ __global__ void __launch_bounds__(RED_THREADS, 2) k_pcg_gather_update(
     }
   }
   __syncthreads();
-  if (threadIdx.x < KR * GU_USED) {
-    const int j = threadIdx.x / GU_USED, qq = threadIdx.x % GU_USED;
+  // all GU_NQ slots are written (the unused ones as zero), so the last block
+  // never reads partial memory that no block has written
+  if (threadIdx.x < KR * GU_NQ) {
+    const int j = threadIdx.x / GU_NQ, qq = threadIdx.x % GU_NQ;
     double v = 0.0;
-    for (int w = 0; w < RED_THREADS / 32; ++w) v = (qq == 4) ? fmax(v, sred[w][j][qq]) : v + sred[w][j][qq];
+    if (qq < GU_USED)
+      for (int w = 0; w < RED_THREADS / 32; ++w) v = (qq == 4) ? fmax(v, sred[w][j][qq]) : v + sred[w][j][qq];
     part[((size_t)blockIdx.x * KR + j) * GU_NQ + qq] = v;
   }
   if (!last_block(&G->cntB)) return;

@@ -9,11 +9,15 @@ small JSON files instead of being recomputed in every test session.
     python tests/golden/make_golden.py slope3d_cut_fos   # ~1 h, 1 core
     python tests/golden/make_golden.py deck_trials       # ~5 min, 1 core
     python tests/golden/make_golden.py slope3d_192k_pcg  # ~1 h, 1 core, 12 GB
+    python tests/golden/make_golden.py excavation_decks  # the reference's excavation decks
 
-tests/golden/decks/ holds two of the reference's own input decks, copied
+tests/golden/decks/ holds some of the reference's own input decks, copied
 unchanged from its input/ folder: validation1 (the slope of its input
-chapter, doc/chap3_input.tex:174-190) and cubit_example (a CUBIT-meshed
-slope with the same material).
+chapter, doc/chap3_input.tex:174-190), cubit_example (a CUBIT-meshed slope
+with the same material), and the excavations excavation_1d (all-elastic, one
+stage, overburden initial stress), excavation_2d (three stages, initial
+stress by the SEM gravity solve) and excavation_2d_single (the same three
+regions removed in one stage, nexcavid = 3).
 """
 from __future__ import annotations
 
@@ -140,6 +144,30 @@ def slope3d_192k_pcg():
     print(json.dumps(out), flush=True)
     with open(os.path.join(HERE, "slope3d_192k_pcg.json"), "w") as f:
         json.dump(out, f, indent=1)
+
+
+def excavation_decks():
+    """The reference's excavation decks run by the oracle as the deck says
+    (stress0 line, nexcav / nexcavid / excavid, ninc): the stage rows
+    [stage, cg_tot, nl_tot, uxmax, umax, fmax, failed, errcode] and the time
+    of each run, so that the GPU's sg_excavation on the same decks can be
+    compared without the CPU time."""
+    import specfem3d_geotech_gb300 as sg
+    out = {}
+    for name in ("excavation_1d", "excavation_2d", "excavation_2d_single"):
+        deck = os.path.join(HERE, "decks", name + ".sem")
+        d = sg.read_deck(deck)
+        om = OracleModel(deck=deck)
+        t0 = time.time()
+        rows = om.excavation(int(d["s0_type"]), float(d["z0"]), float(d["s0"]), float(d["k0"]),
+                             [int(v) for v in d["excavid"]], ninc=int(d["ninc"]),
+                             nexcavid=[int(v) for v in d["nexcavid"]])
+        out[name] = dict(nelmt=om.nelmt, neq=om.neq, s0_type=int(d["s0_type"]), nexcav=int(d["nexcav"]),
+                         excavid=[int(v) for v in d["excavid"]], nexcavid=[int(v) for v in d["nexcavid"]],
+                         ninc=int(d["ninc"]), stages=rows.tolist(), oracle_seconds=time.time() - t0)
+        print(name, json.dumps(out[name]), flush=True)
+        with open(os.path.join(HERE, "excavation_decks.json"), "w") as f:
+            json.dump(out, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -163,13 +163,23 @@ def test_psem_deck_reads_its_unpartitioned_inputs(tmp_path):
         assert np.array_equal(a[k], b[k]), k
 
 
-@pytest.mark.parametrize("name", ["validation1", "cubit_example"])
+@pytest.mark.parametrize("name", ["validation1", "cubit_example", "excavation_1d", "excavation_2d",
+                                  "excavation_2d_single"])
 def test_reference_decks_read_like_the_oracle(name):
-    """Two of the reference's own decks (tests/golden/decks, copied from its
+    """Some of the reference's own decks (tests/golden/decks, copied from its
     input/ folder): CUBIT-exported coordinates, connectivity and side-set
-    boundary files are merged and numbered exactly as the oracle does."""
+    boundary files are merged and numbered exactly as the oracle does, and
+    the excavation decks' stress0 and stage lines are read as the reference
+    reads them (the stress0 line's usek0 key is read and unused, as in the
+    reference)."""
     import os
     deck = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks", name + ".sem")
     r = sg.read_deck(deck)
     _same_mesh(r, OracleModel(deck=deck))
-    assert r["nelmt"] == {"validation1": 1670, "cubit_example": 1690}[name]
+    assert r["nelmt"] == {"validation1": 1670, "cubit_example": 1690, "excavation_1d": 640, "excavation_2d": 1000,
+                          "excavation_2d_single": 1000}[name]
+    if name.startswith("excavation"):
+        stage = {"excavation_1d": (1, [2], [1], 1, 40.0), "excavation_2d": (0, [2, 3, 4], [1, 1, 1], 1, 0.0),
+                 "excavation_2d_single": (0, [2, 3, 4], [3], 1, 0.0)}[name]
+        assert (r["s0_type"], list(r["excavid"]), list(r["nexcavid"]), r["ninc"], r["z0"]) == stage
+        assert r["k0"] == 0.5

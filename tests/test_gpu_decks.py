@@ -10,6 +10,9 @@ product's deck reader (sg_model_from_deck) and run on the device.
   of the same decks (tests/golden/deck_trials.json, made by
   tests/golden/make_golden.py deck_trials): equal plastic-iteration counts,
   PCG totals within 1 %, displacement maxima within the trial tolerance.
+* the reference's excavation decks (excavation_1d, excavation_2d and
+  excavation_2d_single) through sg_excavation as the decks specify them,
+  against the oracle's runs (tests/golden/excavation_decks.json);
 * validation1's own SRF list (1.0 1.5 2.0 2.15 ... 2.20) through
   sg_srf_sweep, the way the reference runs the deck (src/slope.F90:244-443):
   every listed SRF converges, and the plastic iterations climb through the
@@ -74,3 +77,37 @@ def test_validation1_srf_list_sweep(ctx):
     # the knee: the last step of the list costs several times the first step of the bracket
     assert nl[-1] > 3 * nl[3], nl
     m.close()
+
+
+@pytest.fixture(scope="module")
+def oracle_excavations():
+    with open(os.path.join(HERE, "golden", "excavation_decks.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("name", ["excavation_1d", "excavation_2d", "excavation_2d_single"])
+def test_reference_excavation_decks_match_oracle(ctx, oracle_excavations, name):
+    """The reference's excavation decks as they are written (stress0 line,
+    nexcav / nexcavid / excavid, ninc, all-elastic flag) through the deck
+    reader and sg_excavation, against the oracle's runs of the same decks
+    (tests/golden/excavation_decks.json): the same stages, plastic-iteration
+    totals and failure flags, PCG totals within 1 %, displacement maxima
+    within the trial tolerance."""
+    gold = oracle_excavations.get(name)
+    if gold is None:
+        pytest.skip(f"no oracle record for {name}")
+    deck = os.path.join(DECKS, name + ".sem")
+    d = sg.read_deck(deck)
+    m = sg.Model(deck=deck, ctx=ctx)
+    _, ctl = _control(m)
+    rows = m.excavation(ctl, int(d["s0_type"]), float(d["z0"]), float(d["s0"]), float(d["k0"]),
+                        [int(v) for v in d["excavid"]], nexcavid=[int(v) for v in d["nexcavid"]],
+                        ninc=int(d["ninc"]))
+    m.close()
+    ro = np.array(gold["stages"])
+    assert rows.shape == ro.shape
+    assert np.array_equal(rows[:, 0], ro[:, 0])
+    assert np.array_equal(rows[:, 2], ro[:, 2]), (rows[:, 2], ro[:, 2])   # plastic iterations
+    assert np.array_equal(rows[:, 6], ro[:, 6])                           # failed flags
+    assert np.all(np.abs(rows[:, 1] - ro[:, 1]) <= np.maximum(3, 0.01 * ro[:, 1])), (rows[:, 1], ro[:, 1])
+    assert np.allclose(rows[:, 3:5], ro[:, 3:5], rtol=TRIAL_TOL, atol=0), (rows[:, 3:5], ro[:, 3:5])
