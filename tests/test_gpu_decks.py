@@ -32,6 +32,11 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 DECKS = os.path.join(HERE, "golden", "decks")
 TRIAL_TOL = 5e-8     # a whole FP64 trial (the oracle's own reordering noise floor is 4e-8)
+# excavation_2d's third stage runs 172 plastic iterations to nl_tol = 1e-5; the
+# oracle's own dot-product orders (sequential, pairwise, strided, reverse)
+# spread its uxmax and umax there by 8.9e-8 (stage 1: 1.6e-8), so the
+# excavation decks are compared at about twice that
+EXC_TOL = 2e-7
 
 
 @pytest.fixture(scope="module")
@@ -92,7 +97,7 @@ def test_reference_excavation_decks_match_oracle(ctx, oracle_excavations, name):
     reader and sg_excavation, against the oracle's runs of the same decks
     (tests/golden/excavation_decks.json): the same stages, plastic-iteration
     totals and failure flags, PCG totals within 1 %, displacement maxima
-    within the trial tolerance."""
+    within EXC_TOL."""
     gold = oracle_excavations.get(name)
     if gold is None:
         pytest.skip(f"no oracle record for {name}")
@@ -110,4 +115,5 @@ def test_reference_excavation_decks_match_oracle(ctx, oracle_excavations, name):
     assert np.array_equal(rows[:, 2], ro[:, 2]), (rows[:, 2], ro[:, 2])   # plastic iterations
     assert np.array_equal(rows[:, 6], ro[:, 6])                           # failed flags
     assert np.all(np.abs(rows[:, 1] - ro[:, 1]) <= np.maximum(3, 0.01 * ro[:, 1])), (rows[:, 1], ro[:, 1])
-    assert np.allclose(rows[:, 3:5], ro[:, 3:5], rtol=TRIAL_TOL, atol=0), (rows[:, 3:5], ro[:, 3:5])
+    err = np.abs(rows[:, 3:5] - ro[:, 3:5]) / np.abs(ro[:, 3:5])
+    assert err.max() <= EXC_TOL, err
