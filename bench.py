@@ -404,9 +404,12 @@ def admission_report(res, workers, budget):
         a, s = r["t_arrival"], r["t_start"]
         if s - a < 1e-3:
             continue
-        # idle worker at some start event inside the wait (other requests' finishes)
-        for _, b, _ in iv:
-            if a <= b < s and sum(1 for x, y, _ in iv if x <= b < y) < workers:
+        # a worker was idle at some moment of the wait: just after the
+        # arrival or just after another request finished (50 ms margin, so
+        # that a request starting at that finish counts as taking the worker)
+        for b in [a] + [y for _, y, _ in iv if a <= y]:
+            t = b + 0.05
+            if t < s and sum(1 for x, y, _ in iv if x <= t < y) < workers:
                 held += 1
                 break
     return {"budget_gb": budget / 1e9, "peak_running_footprint_gb": peak / 1e9,
