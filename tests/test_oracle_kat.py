@@ -365,3 +365,26 @@ def test_strength_reduction_and_time_step_closed_form():
     ref = min(4 * (1 + nuf[b]) * (1 - 2 * nuf[b]) / (ym[b] * (1 - 2 * nuf[b] + math.sin(phif[b] * d) ** 2))
               for b in range(3))
     assert abs(dt - ref) <= 1e-15 * ref
+
+
+def test_reference_excavation_1d_deck_uplift_closed_form():
+    """The reference's own excavation_1d deck (tests/golden/decks): a 20 x 100
+    x 40 m block with its sides held normal and its base fixed, all-elastic,
+    overburden initial stress from z0 = 40 (gamma = 1, E = 1e4, nu = 0.2), and
+    the top 20 m (material 2) removed in one stage.  The release load is the
+    overburden on the new surface, gamma * 20, and the laterally confined
+    20 m column left below heaves by gamma * h * H / M with the constrained
+    modulus M = E (1 - nu) / ((1 + nu)(1 - 2 nu)): 20 * 20 / 11111.1 =
+    0.036 m.  The oracle, reading the deck as the reference does, gives it."""
+    import specfem3d_geotech_gb300 as sg
+    deck = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks", "excavation_1d.sem")
+    d = sg.read_deck(deck)
+    om = OracleModel(deck=deck)
+    rows = om.excavation(int(d["s0_type"]), float(d["z0"]), float(d["s0"]), float(d["k0"]),
+                         [int(v) for v in d["excavid"]], ninc=int(d["ninc"]),
+                         nexcavid=[int(v) for v in d["nexcavid"]])
+    E, nu, gam, h, H = 1e4, 0.2, 1.0, 20.0, 20.0
+    M = E * (1 - nu) / ((1 + nu) * (1 - 2 * nu))
+    exact = gam * h * H / M
+    assert rows.shape == (1, 8) and rows[0, 6] == 0
+    assert abs(rows[0, 4] - exact) <= 1e-9 * exact, (rows[0, 4], exact)
