@@ -542,7 +542,7 @@ def end_to_end(sg, ctx, mesh, srf, k, args, s_mixed, world):
     """The same work through the public API from host buffers: mesh H2D,
     device model build, the k trials for e2e_steps plastic iterations and the
     k displacement vectors copied back (the drop-in's result, x)."""
-    e2e_steps = max(2, args.steps // 2)
+    e2e_steps = max(3, args.steps)
     ctl = sg.make_control(cg_tol=1e-8, nl_tol=1e-4, cg_maxiter=5000, nl_maxiter=e2e_steps, precision=sg.PREC_MIXED)
     t0 = time.perf_counter()
     me = sg.Model(mesh, precision=sg.PREC_MIXED, ctx=ctx)
