@@ -10,6 +10,7 @@ small JSON files instead of being recomputed in every test session.
     python tests/golden/make_golden.py deck_trials       # ~5 min, 1 core
     python tests/golden/make_golden.py slope3d_192k_pcg  # ~1 h, 1 core, 12 GB
     python tests/golden/make_golden.py excavation_decks  # the reference's excavation decks
+    python tests/golden/make_golden.py water_deck_trials # validation3 / validation4, ~6 min
 
 tests/golden/decks/ holds some of the reference's own input decks, copied
 unchanged from its input/ folder: validation1 (the slope of its input
@@ -17,7 +18,9 @@ chapter, doc/chap3_input.tex:174-190), cubit_example (a CUBIT-meshed slope
 with the same material), and the excavations excavation_1d (all-elastic, one
 stage, overburden initial stress), excavation_2d (three stages, initial
 stress by the SEM gravity solve) and excavation_2d_single (the same three
-regions removed in one stage, nexcavid = 3).
+regions removed in one stage, nexcavid = 3), and validation3 / validation4
+(a slope with a weak layer and a two-surface water table; validation4 adds
+a pseudo-static load).
 """
 from __future__ import annotations
 
@@ -99,17 +102,17 @@ def slope3d_cut_fos():
         json.dump(out, f, indent=1)
 
 
-def deck_trials():
+def deck_trials(names=("validation1", "cubit_example"), srfs=(1.0, 1.5, 2.0), fname="deck_trials.json"):
     """The reference's validation1 and cubit_example decks read by the
     oracle's deck reader: trials at the decks' first three SRFs (1.0, 1.5,
     2.0) with their summaries and the last two uerr values, so that the GPU
     runs of the same decks can be compared with the oracle."""
     out = {}
-    for name in ("validation1", "cubit_example"):
+    for name in names:
         om = OracleModel(deck=os.path.join(HERE, "decks", name + ".sem"))
         rows = []
         t0 = time.time()
-        for s in (1.0, 1.5, 2.0):
+        for s in srfs:
             r = om.trial(s, want_log=True)
             ue = r.pop("uerr_log")
             r.pop("nl_cg")
@@ -119,8 +122,15 @@ def deck_trials():
             print(name, json.dumps(r), flush=True)
         out[name] = dict(nelmt=om.nelmt, neq=om.neq, control={k: (v.tolist() if hasattr(v, "tolist") else v)
                                                                for k, v in om.control().items()}, trials=rows)
-    with open(os.path.join(HERE, "deck_trials.json"), "w") as f:
+    with open(os.path.join(HERE, fname), "w") as f:
         json.dump(out, f, indent=1)
+
+
+def water_deck_trials():
+    """validation3 and validation4 (water table; validation4 with its eqload
+    line) as the reference runs them: the deck's SRF list reads as 1.0 alone
+    (its ntstep= / sf= keys are not the reader's nsrf= / srf=)."""
+    deck_trials(("validation3", "validation4"), (1.0,), "water_deck_trials.json")
 
 
 def slope3d_192k_pcg():

@@ -164,7 +164,7 @@ def test_psem_deck_reads_its_unpartitioned_inputs(tmp_path):
 
 
 @pytest.mark.parametrize("name", ["validation1", "cubit_example", "excavation_1d", "excavation_2d",
-                                  "excavation_2d_single"])
+                                  "excavation_2d_single", "validation3", "validation4"])
 def test_reference_decks_read_like_the_oracle(name):
     """Some of the reference's own decks (tests/golden/decks, copied from its
     input/ folder): CUBIT-exported coordinates, connectivity and side-set
@@ -177,7 +177,11 @@ def test_reference_decks_read_like_the_oracle(name):
     r = sg.read_deck(deck)
     _same_mesh(r, OracleModel(deck=deck))
     assert r["nelmt"] == {"validation1": 1670, "cubit_example": 1690, "excavation_1d": 640, "excavation_2d": 1000,
-                          "excavation_2d_single": 1000}[name]
+                          "excavation_2d_single": 1000, "validation3": 1800, "validation4": 1800}[name]
+    if name in ("validation3", "validation4"):
+        # the water table (wsfile, water materials 2 and 3) and validation4's eqload line
+        assert r["iswater"] == 1 and list(r["water_ids"]) == [2, 3]
+        assert (r["iseqload"], r["eqk"]) == ((1, (0.1, 0.0, 0.0)) if name == "validation4" else (0, (0.0, 0.0, 0.0)))
     if name.startswith("excavation"):
         stage = {"excavation_1d": (1, [2], [1], 1, 40.0), "excavation_2d": (0, [2, 3, 4], [1, 1, 1], 1, 0.0),
                  "excavation_2d_single": (0, [2, 3, 4], [3], 1, 0.0)}[name]

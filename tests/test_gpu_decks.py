@@ -10,6 +10,8 @@ product's deck reader (sg_model_from_deck) and run on the device.
   of the same decks (tests/golden/deck_trials.json, made by
   tests/golden/make_golden.py deck_trials): equal plastic-iteration counts,
   PCG totals within 1 %, displacement maxima within the trial tolerance.
+* the water decks validation3 and validation4 (water table, weak layer,
+  pseudo-static load) at the SRF their reader gives them;
 * the reference's excavation decks (excavation_1d, excavation_2d and
   excavation_2d_single) through sg_excavation as the decks specify them,
   against the oracle's runs (tests/golden/excavation_decks.json);
@@ -117,3 +119,29 @@ def test_reference_excavation_decks_match_oracle(ctx, oracle_excavations, name):
     assert np.all(np.abs(rows[:, 1] - ro[:, 1]) <= np.maximum(3, 0.01 * ro[:, 1])), (rows[:, 1], ro[:, 1])
     err = np.abs(rows[:, 3:5] - ro[:, 3:5]) / np.abs(ro[:, 3:5])
     assert err.max() <= EXC_TOL, err
+
+
+@pytest.mark.parametrize("name", ["validation3", "validation4"])
+def test_reference_water_decks_match_oracle(ctx, name):
+    """The reference's validation3 (a slope with a weak layer, c = 0, and a
+    two-surface water table on materials 2 and 3) and validation4 (the same
+    with its eqload: line, eqkx = 0.1) read as the reference reads them, at
+    the SRF the reader gives them (1.0: their ntstep= / sf= keys are not the
+    reader's nsrf= / srf=): the pore pressure enters the stress block and the
+    pseudo-static load the right-hand side on the device, and the trial
+    equals the oracle's run of the same deck (tests/golden/water_deck_trials.json)."""
+    with open(os.path.join(HERE, "golden", "water_deck_trials.json")) as f:
+        gold = json.load(f).get(name)
+    if gold is None:
+        pytest.skip(f"no oracle record for {name}")
+    m = sg.Model(deck=os.path.join(DECKS, name + ".sem"), ctx=ctx)
+    assert (m.nelmt, m.neq) == (gold["nelmt"], gold["neq"])
+    c, ctl = _control(m)
+    assert list(c["srf"]) == [1.0]
+    for ro in gold["trials"]:
+        r = m.trials([ro["srf"]], ctl)[0]
+        assert r["nl_iter"] == ro["nl_iter"] and r["converged"] == ro["converged"], (r, ro)
+        assert abs(r["cg_tot"] - ro["cg_tot"]) <= max(3, 0.01 * ro["cg_tot"]), (r["cg_tot"], ro["cg_tot"])
+        for k in ("umax", "uxmax"):
+            assert abs(r[k] - ro[k]) <= TRIAL_TOL * abs(ro[k]), (k, r[k], ro[k])
+    m.close()
