@@ -159,3 +159,27 @@ def test_vertical_meshed_face_takes_its_top(tmp_path):
     # upper element's face covers the rest with top z = 2
     ztop = np.where(c[:, 2] <= 1.0, 1.0, 2.0)
     assert np.array_equal(wp, np.where(on_plane, GAMW * (ztop - c[:, 2]), 0.0))
+
+
+def test_reference_validation3_deck_water_table():
+    """The reference's own validation3 deck (tests/golden/decks): its water
+    file holds two surfaces -- a horizontal table z = 6.1 over 42.7 <= x <= 50
+    first, then an inclined one from (0, 12.2) to (42.7, 6.1) -- and materials
+    2 and 3 are the water materials.  Read as the reference reads the deck,
+    every node of those materials has 9.81 (z_s(x) - z) where it lies under
+    the surface and 0 above it, and the nodes of material 1 stay dry."""
+    import os
+    deck = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "decks", "validation3.sem")
+    om = OracleModel(deck=deck)
+    wp, sub = om.pore_pressure()
+    a = om.arrays()
+    c = a["g_coord"].reshape(-1, 3)
+    x, z = c[:, 0], c[:, 2]
+    gnum = a["g_num"].reshape(-1, 27)
+    wet = np.zeros(om.nnode, bool)
+    wet[gnum[np.isin(a["mat_id"], [2, 3])].reshape(-1)] = True
+    assert np.array_equal(sub, wet)
+    zs = np.where(x >= 42.7, 6.1, 12.2 + (6.1 - 12.2) * x / 42.7)
+    expect = np.where(wet, np.maximum(GAMW * (zs - z), 0.0), 0.0)
+    assert np.abs(wp - expect).max() <= 1e-12 * np.abs(expect).max()
+    assert (wp > 0).sum() > 1000 and wp.max() > 100.0
